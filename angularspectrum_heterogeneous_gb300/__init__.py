@@ -1,0 +1,12 @@
+"""GB300-native angular-spectrum march (drop-in for angular_spectrum_solver's solver API).
+
+    from angularspectrum_heterogeneous_gb300 import SolverParams, angular_spectrum_solve
+"""
+from .solver import (ASGError, Plan, SolverParams, StabilityError,  # noqa: F401
+                     angular_spectrum_solve)
+from .sources import (generate_phase_screen, make_bowl_source,  # noqa: F401
+                      make_bowl_source_planes, skull_to_phase_screens)
+
+__all__ = ["SolverParams", "angular_spectrum_solve", "Plan", "ASGError", "StabilityError",
+           "make_bowl_source", "make_bowl_source_planes", "generate_phase_screen",
+           "skull_to_phase_screens"]

@@ -1,0 +1,1180 @@
+// C ABI of the GB300 angular-spectrum march: plan management, operator
+// tables, screens/sources, and the host driver of the march.
+//
+// The driver reproduces the control flow of the reference's
+// angular_spectrum_solve (angular_spectrum_solver.py:1408-1567):
+//   z bookkeeping with sum(zvec) as a sequential double sum, partial last
+//   step (:1413-1415, :1447-1450), stability test before each step (:1418-1420;
+//   an error here, where the reference restarts forever), Strang or Lie
+//   splitting (:1454-1492), freq-weighted and super-absorbing boundaries
+//   (:1495-1502), screens crossed in (z, z+dZ] (:1505-1518), sources crossed
+//   in (z, z+dZ] (:1521-1527), accumulators (:1529-1536), callback
+//   (:1547-1548) and the trimmed outputs (:1556-1567).
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "asg_generic.cuh"
+#include "asg_internal.h"
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                    \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return fail(ASG_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                              \
+  } while (0)
+
+#define CKS(expr)                                                              \
+  do {                                                                         \
+    int s_ = (expr);                                                           \
+    if (s_ != ASG_OK) {                                                        \
+      if (g_err.empty()) fail(s_, "%s failed (%d)", #expr, s_);                \
+      return s_;                                                               \
+    }                                                                          \
+  } while (0)
+
+template <typename T>
+static int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess)
+    return fail(ASG_ERR_NOMEM, "cudaMalloc of %zu bytes failed", n * sizeof(T));
+  return ASG_OK;
+}
+template <typename T>
+static int h2d(T* d, const T* h, size_t n, cudaStream_t st) {
+  CK(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host FFT plan helpers
+// ---------------------------------------------------------------------------
+static GenPlan make_gen_plan(int n) {
+  GenPlan p;
+  memset(&p, 0, sizeof(p));
+  p.n = n;
+  int m = n;
+  const int pref[4] = {8, 4, 2, 3};
+  for (int r : pref) {
+    while (m % r == 0 && p.nrad < 24) {
+      p.rad[p.nrad++] = r;
+      m /= r;
+    }
+  }
+  for (int r = 5; m > 1 && p.nrad < 24; r += 2) {
+    while (m % r == 0) {
+      p.rad[p.nrad++] = r;
+      m /= r;
+    }
+  }
+  return p;
+}
+
+static void roots(int n, std::vector<float2>& out) {
+  out.resize(n);
+  for (int k = 0; k < n; ++k) {
+    const double a = -2.0 * M_PI * (double)k / (double)n;
+    out[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+}
+
+// four-step slot order of a fast line of length n (n = n1*n2)
+static void fast_factors(int n, int* n1, int* n2) {
+  switch (n) {
+    case 64: *n1 = 8; *n2 = 8; break;
+    case 96: *n1 = 8; *n2 = 12; break;
+    case 128: *n1 = 8; *n2 = 16; break;
+    case 192: *n1 = 12; *n2 = 16; break;
+    case 256: *n1 = 16; *n2 = 16; break;
+    case 384: *n1 = 16; *n2 = 24; break;
+    case 512: *n1 = 16; *n2 = 32; break;
+    case 768: *n1 = 24; *n2 = 32; break;
+    case 1024: *n1 = 32; *n2 = 32; break;
+    default: *n1 = 0; *n2 = 0; break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Python's built-in sum() over a list of floats (CPython >= 3.12): the first
+// item enters exactly (0 + x0), later items with Neumaier compensation, and
+// the compensation is added at the end when it is finite and non-zero.  The
+// reference's control flow reads sum(zvec) (:1413-1414, :1506, :1522, :1548).
+// ---------------------------------------------------------------------------
+struct PySum {
+  double f = 0.0, c = 0.0;
+  long n = 0;
+  void add(double x) {
+    if (n == 0) {
+      f = 0.0 + x;
+    } else {
+      const double t = f + x;
+      if (fabs(f) >= fabs(x)) c += (f - t) + x;
+      else c += (x - t) + f;
+      f = t;
+    }
+    ++n;
+  }
+  double value() const {
+    double r = f;
+    if (c != 0.0 && isfinite(c)) r += c;
+    return r;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+struct Slot {
+  bool ready = false;
+  double dz = 0.0;
+  double beta_tvd = 1.0;
+  float2* tabA = nullptr;  // Strang: H(dz/2) A(1/2)  | Lie: H(dz)
+  float2* tabB = nullptr;  // Strang: H(dz/2)
+  float2* tabC = nullptr;  // Strang: A(1/2)          | Lie: A(1)
+  // 1-D vectors kept for single-operator application
+  double* kt_prop = nullptr;
+  double* km_att = nullptr;
+  double* alpha = nullptr;
+  double* astar = nullptr;
+  double kstart = 0, kmax_t = 0;
+  int att_obl = 1, att_clip = 0;
+};
+
+struct Screen {
+  double z;
+  float* phase;
+  float* amp;
+};
+struct Source {
+  double z;
+  int* map;
+  float* val;
+  int nactive;
+};
+
+struct asg_plan {
+  asg_config cfg;
+  int X, Y, T, ncols, F, M;
+  bool tfast, xyfast;
+  int G;
+  GenPlan gp_t, gp_x, gp_y;
+  cudaStream_t st;
+  cudaEvent_t ev0, ev1;
+  float2* spec = nullptr;
+  float* real = nullptr;
+  float2 *twT = nullptr, *twM = nullptr, *twX = nullptr, *twY = nullptr;
+  int *f_of_plane = nullptr, *cls_x = nullptr, *cls_y = nullptr;
+  int ncx, ncy;
+  double *kx2 = nullptr, *ky2 = nullptr;
+  std::vector<int> h_f_of_plane;
+  std::vector<int> h_cls_x, h_cls_y;
+  std::vector<int> h_rep_x, h_rep_y;  // centred-grid index of each class
+  Slot slot[2];
+  float2* tab_scratch = nullptr;
+  // tapers
+  float *abl_xy_half = nullptr, *abl_t_half = nullptr, *abl_xy_full = nullptr,
+        *abl_t_full = nullptr;
+  bool have_ops = false;
+  // epilogue data
+  float *fw_lx = nullptr, *fw_ly = nullptr, *fw_exp = nullptr;
+  float *sa_wx = nullptr, *sa_wy = nullptr, *sa_coef = nullptr;
+  float* screen_fscale = nullptr;
+  float* obl_tab = nullptr;
+  double* power_acc = nullptr;
+  // screens / sources
+  std::vector<Screen> screens;
+  std::vector<Source> sources;
+  ScreenDev* d_screens = nullptr;  // per-step list (max 64)
+  SourceEvent* d_src = nullptr;    // per-step list (max 64)
+  // state
+  int* d_step = nullptr;
+  unsigned *d_max_cur = nullptr, *d_max_next = nullptr, *d_status = nullptr;
+  int* d_status_step = nullptr;
+  double* d_iprev = nullptr;
+  unsigned* d_hist = nullptr;
+  // outputs
+  float *o_pnp = nullptr, *o_ppp = nullptr, *o_pI = nullptr, *o_pIloss = nullptr, *o_pax = nullptr;
+  int o_cap = 0;
+  std::vector<double> zaxis;
+  int nsteps = 0;
+  double run_ms = 0.0;
+  double N = 0.0;
+  // per-kernel accounting: launch counts always, CUDA-event times when enabled
+  bool prof = false;
+  long launches[ASG_NKINDS] = {0};
+  double kms[ASG_NKINDS] = {0};
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kind;  // kind of event pair i (events 2i, 2i+1)
+};
+
+// launch accounting around one kernel launch of `kind`
+struct KScope {
+  asg_plan* p;
+  int kind;
+  KScope(asg_plan* p_, int k) : p(p_), kind(k) {
+    p->launches[kind]++;
+    if (p->prof) {
+      const size_t i = p->ev_kind.size();
+      while (p->ev_pool.size() < 2 * (i + 1)) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        p->ev_pool.push_back(e);
+      }
+      p->ev_kind.push_back(kind);
+      cudaEventRecord(p->ev_pool[2 * i], p->st);
+    }
+  }
+  ~KScope() {
+    if (p->prof) cudaEventRecord(p->ev_pool[2 * (p->ev_kind.size() - 1) + 1], p->st);
+  }
+};
+
+static void collect_kernel_times(asg_plan* p) {
+  if (!p->prof) return;
+  cudaStreamSynchronize(p->st);
+  for (size_t i = 0; i < p->ev_kind.size(); ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p->ev_pool[2 * i], p->ev_pool[2 * i + 1]) == cudaSuccess)
+      p->kms[p->ev_kind[i]] += ms;
+  }
+  p->ev_kind.clear();
+}
+
+static void free_slot(Slot& s) {
+  cudaFree(s.tabA);
+  cudaFree(s.tabB);
+  cudaFree(s.tabC);
+  cudaFree(s.kt_prop);
+  cudaFree(s.km_att);
+  cudaFree(s.alpha);
+  cudaFree(s.astar);
+  s = Slot();
+}
+
+static void free_outputs(asg_plan* p) {
+  cudaFree(p->o_pnp);
+  cudaFree(p->o_ppp);
+  cudaFree(p->o_pI);
+  cudaFree(p->o_pIloss);
+  cudaFree(p->o_pax);
+  p->o_pnp = p->o_ppp = p->o_pI = p->o_pIloss = p->o_pax = nullptr;
+  p->o_cap = 0;
+}
+
+extern "C" int asg_plan_destroy(asg_plan* p) {
+  if (!p) return ASG_OK;
+  cudaStreamSynchronize(p->st);
+  for (auto& s : p->slot) free_slot(s);
+  for (auto& s : p->screens) {
+    cudaFree(s.phase);
+    cudaFree(s.amp);
+  }
+  for (auto& s : p->sources) {
+    cudaFree(s.map);
+    cudaFree(s.val);
+  }
+  void* ptrs[] = {p->spec, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+                  p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
+                  p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
+                  p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
+                  p->d_screens, p->d_src, p->d_step, p->d_max_cur, p->d_max_next,
+                  p->d_status, p->d_status_step, p->d_iprev, p->d_hist};
+  for (void* q : ptrs) cudaFree(q);
+  free_outputs(p);
+  cudaEventDestroy(p->ev0);
+  cudaEventDestroy(p->ev1);
+  for (auto e : p->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(p->st);
+  delete p;
+  return ASG_OK;
+}
+
+static bool g_roots_done = false;
+static int upload_roots() {
+  if (g_roots_done) return ASG_OK;
+  std::vector<float2> w192, w64;
+  roots(192, w192);
+  roots(64, w64);
+  if (asg_roots_upload_t(w192.data(), w64.data()) != 0 ||
+      asg_roots_upload_xy(w192.data(), w64.data()) != 0)
+    return fail(ASG_ERR_CUDA, "upload of the constant root tables failed");
+  g_roots_done = true;
+  return ASG_OK;
+}
+
+static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
+  p->cfg = *cfg;
+  const int X = cfg->nX, Y = cfg->nY, T = cfg->nT;
+  if (X < 2 || Y < 2 || T < 3) return fail(ASG_ERR_SHAPE, "grid %dx%dx%d too small", X, Y, T);
+  p->X = X;
+  p->Y = Y;
+  p->T = T;
+  p->ncols = X * Y;
+  p->F = T / 2 + 1;
+  p->M = T / 2;
+  p->N = cfg->beta / (2.0 * cfg->c0 * cfg->c0 * cfg->c0 * cfg->rho0);
+  p->tfast = asg_t_fast_supported(T);
+  p->xyfast = asg_xy_fast_supported(X, Y, &p->G);
+  if (!p->xyfast) {
+    p->G = 1;
+    if (asg_xy_generic_smem(X, Y) > 200 * 1024)
+      return fail(ASG_ERR_SHAPE,
+                  "grid %dx%d: no fast plane transform (needs nX = 32*G, G in "
+                  "{1,2,3,4,6,8,12,16}, nY in {64,96,128,192,256,384,512}) and the plane is too "
+                  "large for the generic in-shared-memory transform",
+                  X, Y);
+  }
+  if (!p->tfast && asg_t_generic_smem(T) > 200 * 1024)
+    return fail(ASG_ERR_SHAPE, "nT=%d too long for the generic column transform", T);
+  if (!p->tfast && (T + 31) / 32 > 64)
+    return fail(ASG_ERR_SHAPE, "nT=%d too long for the generic column transform", T);
+  if (Y > 1024) return fail(ASG_ERR_SHAPE, "nY=%d > 1024", Y);
+  p->gp_t = make_gen_plan(T);
+  p->gp_x = make_gen_plan(X);
+  p->gp_y = make_gen_plan(Y);
+  CK(cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&p->ev0));
+  CK(cudaEventCreate(&p->ev1));
+  CKS(upload_roots());
+
+  // ---- planes ----
+  p->h_f_of_plane.resize(p->F);
+  if (p->tfast) {
+    int n1, n2;
+    fast_factors(p->M, &n1, &n2);
+    for (int q = 0; q < p->M; ++q) p->h_f_of_plane[q] = (q / n2) + n1 * (q % n2);
+    p->h_f_of_plane[p->M] = p->M;
+  } else {
+    for (int q = 0; q < p->F; ++q) p->h_f_of_plane[q] = q;
+  }
+  // ---- x/y slot -> natural bin, and mirror classes ----
+  auto slot_bins = [](int n, bool fast_xy_x, bool fast_y, int G, std::vector<int>& bin) {
+    bin.resize(n);
+    for (int s = 0; s < n; ++s) {
+      if (fast_xy_x) {
+        const int R = n / G;
+        bin[s] = (s / R) + G * (s % R);
+      } else if (fast_y) {
+        int n1, n2;
+        fast_factors(n, &n1, &n2);
+        bin[s] = (s / n2) + n1 * (s % n2);
+      } else {
+        bin[s] = s;
+      }
+    }
+  };
+  std::vector<int> binx, biny;
+  slot_bins(X, p->xyfast, false, p->G, binx);
+  slot_bins(Y, false, p->xyfast, 1, biny);
+  // mirror classes: slots whose bins sit at centred-grid positions i and
+  // n-1-i share k^2 (the reference's centred grid is symmetric); class id =
+  // the smaller slot of the pair, so consecutive slots read consecutive
+  // table entries
+  auto classes = [](int n, const std::vector<int>& bin, std::vector<int>& cls, int& ncls,
+                    std::vector<int>& rep) {
+    std::vector<int> slot_of_cent(n), cent(n);
+    for (int s = 0; s < n; ++s) {
+      cent[s] = (bin[s] + n / 2) % n;
+      slot_of_cent[cent[s]] = s;
+    }
+    std::vector<int> raw(n), id(n, -1);
+    for (int s = 0; s < n; ++s) {
+      const int s2 = slot_of_cent[n - 1 - cent[s]];
+      raw[s] = s < s2 ? s : s2;
+    }
+    ncls = 0;
+    rep.clear();
+    for (int s = 0; s < n; ++s)
+      if (raw[s] == s) {
+        id[s] = ncls++;
+        rep.push_back(cent[s]);
+      }
+    cls.resize(n);
+    for (int s = 0; s < n; ++s) cls[s] = id[raw[s]];
+  };
+  classes(X, binx, p->h_cls_x, p->ncx, p->h_rep_x);
+  classes(Y, biny, p->h_cls_y, p->ncy, p->h_rep_y);
+
+  // ---- device buffers ----
+  const size_t nspec = (size_t)p->F * p->ncols;
+  CKS(dalloc(&p->spec, nspec));
+  CKS(dalloc(&p->real, (size_t)p->ncols * T));
+  std::vector<float2> w;
+  roots(T, w);
+  CKS(dalloc(&p->twT, T));
+  CKS(h2d(p->twT, w.data(), T, p->st));
+  roots(p->M > 0 ? p->M : 1, w);
+  CKS(dalloc(&p->twM, w.size()));
+  CKS(h2d(p->twM, w.data(), w.size(), p->st));
+  roots(X, w);
+  CKS(dalloc(&p->twX, X));
+  CKS(h2d(p->twX, w.data(), X, p->st));
+  roots(Y, w);
+  CKS(dalloc(&p->twY, Y));
+  CKS(h2d(p->twY, w.data(), Y, p->st));
+  CKS(dalloc(&p->f_of_plane, p->F));
+  CKS(h2d(p->f_of_plane, p->h_f_of_plane.data(), p->F, p->st));
+  CKS(dalloc(&p->cls_x, X));
+  CKS(h2d(p->cls_x, p->h_cls_x.data(), X, p->st));
+  CKS(dalloc(&p->cls_y, Y));
+  CKS(h2d(p->cls_y, p->h_cls_y.data(), Y, p->st));
+  CKS(dalloc(&p->kx2, p->ncx));
+  CKS(dalloc(&p->ky2, p->ncy));
+  const size_t ntab = (size_t)p->F * p->ncx * p->ncy;
+  CKS(dalloc(&p->tab_scratch, ntab));
+  CKS(dalloc(&p->abl_xy_half, p->ncols));
+  CKS(dalloc(&p->abl_xy_full, p->ncols));
+  CKS(dalloc(&p->abl_t_half, T));
+  CKS(dalloc(&p->abl_t_full, T));
+  CKS(dalloc(&p->fw_lx, X));
+  CKS(dalloc(&p->fw_ly, Y));
+  CKS(dalloc(&p->fw_exp, p->F));
+  CKS(dalloc(&p->sa_wx, X));
+  CKS(dalloc(&p->sa_wy, Y));
+  CKS(dalloc(&p->sa_coef, p->F));
+  CKS(dalloc(&p->screen_fscale, p->F));
+  CKS(dalloc(&p->power_acc, 2));
+  CKS(dalloc(&p->d_screens, 64));
+  CKS(dalloc(&p->d_src, 64));
+  CKS(dalloc(&p->d_step, 1));
+  CKS(dalloc(&p->d_max_cur, 1));
+  CKS(dalloc(&p->d_max_next, 1));
+  CKS(dalloc(&p->d_status, 1));
+  CKS(dalloc(&p->d_status_step, 1));
+  CKS(dalloc(&p->d_iprev, p->ncols));
+  CKS(dalloc(&p->d_hist, 64));
+  CK(cudaMemsetAsync(p->d_status, 0, sizeof(unsigned), p->st));
+  CK(cudaMemsetAsync(p->d_hist, 0, 64 * sizeof(unsigned), p->st));
+
+  // per-plane constants that do not depend on the step
+  {
+    const double dT = cfg->dT;
+    std::vector<float> sac(p->F), fsc(p->F);
+    const double w1 = 2.0 * M_PI * (1.0 / (T * dT));  // omega of bin 1
+    const double f0_bin = cfg->f0 / (1.0 / (T * dT));
+    for (int q = 0; q < p->F; ++q) {
+      const int f = p->h_f_of_plane[q];
+      const double om = 2.0 * M_PI * ((double)f / (T * dT));
+      sac[q] = (fabs(om) > 0.5 * w1) ? (float)(cfg->c0 / om) : 0.f;
+      fsc[q] = (float)((double)(float)f / fmax(f0_bin, 1.0));
+    }
+    CKS(h2d(p->sa_coef, sac.data(), p->F, p->st));
+    CKS(h2d(p->screen_fscale, fsc.data(), p->F, p->st));
+  }
+  CK(cudaStreamSynchronize(p->st));
+  return ASG_OK;
+}
+
+extern "C" int asg_plan_create(const asg_config* cfg, asg_plan** out) {
+  g_err.clear();
+  if (!cfg || !out) return fail(ASG_ERR_ARG, "null argument");
+  asg_plan* p = new asg_plan();
+  int s = plan_create_impl(cfg, p);
+  if (s != ASG_OK) {
+    std::string e = g_err;
+    asg_plan_destroy(p);
+    g_err = e;
+    *out = nullptr;
+    return s;
+  }
+  *out = p;
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// operators
+// ---------------------------------------------------------------------------
+static int build_table(asg_plan* p, Slot& s, float2* out, bool prop, double dz_prop, bool att,
+                       double dz_att) {
+  TableParams tp;
+  memset(&tp, 0, sizeof(tp));
+  tp.nplanes = p->F;
+  tp.ncx = p->ncx;
+  tp.ncy = p->ncy;
+  tp.kx2 = p->kx2;
+  tp.ky2 = p->ky2;
+  tp.kt_prop = s.kt_prop;
+  tp.km_att = s.km_att;
+  tp.alpha = s.alpha;
+  tp.astar = s.astar;
+  tp.f_of_plane = p->f_of_plane;
+  tp.nT = p->T;
+  tp.dz_prop = dz_prop;
+  tp.dz_att = dz_att;
+  tp.kstart = s.kstart;
+  tp.kmax_t = s.kmax_t;
+  tp.use_prop = prop;
+  tp.use_att = att;
+  tp.obliquity = s.att_obl;
+  tp.clip_negative = s.att_clip;
+  tp.norm = 1.0 / ((double)p->X * (double)p->Y);
+  tp.out = out;
+  return asg_launch_table(tp, p->st);
+}
+
+extern "C" int asg_set_step_operators(asg_plan* p, int slot, const asg_step_operators* o) {
+  g_err.clear();
+  if (!p || !o || slot < 0 || slot > 1) return fail(ASG_ERR_ARG, "bad argument");
+  if (!o->kx || !o->ky || !o->kt || !o->alpha || !o->alpha_star || !o->abl_x || !o->abl_y ||
+      !o->abl_t)
+    return fail(ASG_ERR_ARG, "missing operator vector");
+  const int X = p->X, Y = p->Y, T = p->T, F = p->F;
+  Slot& s = p->slot[slot];
+  s.dz = o->dz;
+  s.beta_tvd = o->beta_tvd;
+  s.kstart = o->kfilt_start;
+  s.kmax_t = o->kfilt_max;
+  s.att_obl = o->atten_obliquity;
+  s.att_clip = o->atten_clip_negative;
+  // class wavenumbers (shared by both slots)
+  {
+    std::vector<double> kx2(p->ncx), ky2(p->ncy);
+    for (int c = 0; c < p->ncx; ++c) kx2[c] = o->kx[p->h_rep_x[c]] * o->kx[p->h_rep_x[c]];
+    for (int c = 0; c < p->ncy; ++c) ky2[c] = o->ky[p->h_rep_y[c]] * o->ky[p->h_rep_y[c]];
+    CKS(h2d(p->kx2, kx2.data(), p->ncx, p->st));
+    CKS(h2d(p->ky2, ky2.data(), p->ncy, p->st));
+  }
+  // per-plane vectors
+  std::vector<double> ktp(F), kma(F), al(F), as(F);
+  for (int q = 0; q < F; ++q) {
+    const int f = p->h_f_of_plane[q];
+    ktp[q] = o->kt[(f + T / 2) % T];
+    kma[q] = 2.0 * M_PI * ((double)f / (T * p->cfg.dT)) / p->cfg.c0;
+    al[q] = o->alpha[f];
+    as[q] = o->alpha_star[f];
+  }
+  if (!s.kt_prop) {
+    CKS(dalloc(&s.kt_prop, F));
+    CKS(dalloc(&s.km_att, F));
+    CKS(dalloc(&s.alpha, F));
+    CKS(dalloc(&s.astar, F));
+  }
+  CKS(h2d(s.kt_prop, ktp.data(), F, p->st));
+  CKS(h2d(s.km_att, kma.data(), F, p->st));
+  CKS(h2d(s.alpha, al.data(), F, p->st));
+  CKS(h2d(s.astar, as.data(), F, p->st));
+  const size_t ntab = (size_t)F * p->ncx * p->ncy;
+  if (!s.tabA) {
+    CKS(dalloc(&s.tabA, ntab));
+    CKS(dalloc(&s.tabC, ntab));
+    if (p->cfg.split_step) CKS(dalloc(&s.tabB, ntab));
+  }
+  const double dz = o->dz;
+  if (p->cfg.split_step) {
+    CKS(build_table(p, s, s.tabA, true, dz / 2, true, dz * 0.5));
+    CKS(build_table(p, s, s.tabB, true, dz / 2, false, 0.0));
+    CKS(build_table(p, s, s.tabC, false, 0.0, true, dz * 0.5));
+  } else {
+    CKS(build_table(p, s, s.tabA, true, dz, false, 0.0));
+    CKS(build_table(p, s, s.tabC, false, 0.0, true, dz * 1.0));
+  }
+  // tapers (slot independent)
+  {
+    std::vector<float> axh(p->ncols), axf(p->ncols), ath(T), atf(T);
+    for (int x = 0; x < X; ++x)
+      for (int y = 0; y < Y; ++y) {
+        const double v = o->abl_x[x] * o->abl_y[y];
+        axf[(size_t)x * Y + y] = (float)v;
+        axh[(size_t)x * Y + y] = (float)sqrt(v);
+      }
+    for (int t = 0; t < T; ++t) {
+      atf[t] = (float)o->abl_t[t];
+      ath[t] = (float)sqrt(o->abl_t[t]);
+    }
+    CKS(h2d(p->abl_xy_half, axh.data(), p->ncols, p->st));
+    CKS(h2d(p->abl_xy_full, axf.data(), p->ncols, p->st));
+    CKS(h2d(p->abl_t_half, ath.data(), T, p->st));
+    CKS(h2d(p->abl_t_full, atf.data(), T, p->st));
+  }
+  // freq-weighted mask factors
+  if (o->fw_exponent && o->fw_taper_x && o->fw_taper_y) {
+    std::vector<float> lx(X), ly(Y), fe(F);
+    for (int x = 0; x < X; ++x) lx[x] = (float)log2(o->fw_taper_x[x]);
+    for (int y = 0; y < Y; ++y) ly[y] = (float)log2(o->fw_taper_y[y]);
+    for (int q = 0; q < F; ++q) fe[q] = (float)o->fw_exponent[p->h_f_of_plane[q]];
+    CKS(h2d(p->fw_lx, lx.data(), X, p->st));
+    CKS(h2d(p->fw_ly, ly.data(), Y, p->st));
+    CKS(h2d(p->fw_exp, fe.data(), F, p->st));
+  }
+  if (o->sa_wx && o->sa_wy) {
+    std::vector<float> wx(X), wy(Y);
+    for (int x = 0; x < X; ++x) wx[x] = (float)o->sa_wx[x];
+    for (int y = 0; y < Y; ++y) wy[y] = (float)o->sa_wy[y];
+    CKS(h2d(p->sa_wx, wx.data(), X, p->st));
+    CKS(h2d(p->sa_wy, wy.data(), Y, p->st));
+  }
+  if (p->cfg.nonlinear_obliquity && !p->obl_tab) {
+    CKS(dalloc(&p->obl_tab, ntab));
+    TableParams tp;
+    memset(&tp, 0, sizeof(tp));
+    tp.nplanes = F;
+    tp.ncx = p->ncx;
+    tp.ncy = p->ncy;
+    tp.kx2 = p->kx2;
+    tp.ky2 = p->ky2;
+    tp.km_att = s.km_att;
+    CKS(asg_launch_obl_table(tp, p->obl_tab, p->st));
+  }
+  CK(cudaStreamSynchronize(p->st));
+  s.ready = true;
+  if (slot == 0) p->have_ops = true;
+  return ASG_OK;
+}
+
+extern "C" int asg_add_screen(asg_plan* p, double z, const float* phase, const float* amp) {
+  g_err.clear();
+  if (!p || !phase) return fail(ASG_ERR_ARG, "null argument");
+  Screen s;
+  s.z = z;
+  s.phase = nullptr;
+  s.amp = nullptr;
+  CKS(dalloc(&s.phase, p->ncols));
+  CK(cudaMemcpy(s.phase, phase, p->ncols * sizeof(float), cudaMemcpyHostToDevice));
+  if (amp) {
+    CKS(dalloc(&s.amp, p->ncols));
+    CK(cudaMemcpy(s.amp, amp, p->ncols * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  p->screens.push_back(s);
+  return ASG_OK;
+}
+
+extern "C" int asg_add_source(asg_plan* p, double z, const float* plane) {
+  g_err.clear();
+  if (!p || !plane) return fail(ASG_ERR_ARG, "null argument");
+  const int T = p->T;
+  std::vector<int> map(p->ncols, -1);
+  std::vector<float> vals;
+  int na = 0;
+  for (int c = 0; c < p->ncols; ++c) {
+    const float* col = plane + (size_t)c * T;
+    bool nz = false;
+    for (int t = 0; t < T; ++t)
+      if (col[t] != 0.f) {
+        nz = true;
+        break;
+      }
+    if (nz) {
+      map[c] = na++;
+      vals.insert(vals.end(), col, col + T);
+    }
+  }
+  Source s;
+  s.z = z;
+  s.nactive = na;
+  s.map = nullptr;
+  s.val = nullptr;
+  CKS(dalloc(&s.map, p->ncols));
+  CK(cudaMemcpy(s.map, map.data(), p->ncols * sizeof(int), cudaMemcpyHostToDevice));
+  CKS(dalloc(&s.val, (size_t)(na > 0 ? na : 1) * T));
+  if (na > 0)
+    CK(cudaMemcpy(s.val, vals.data(), vals.size() * sizeof(float), cudaMemcpyHostToDevice));
+  p->sources.push_back(s);
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernel parameter helpers
+// ---------------------------------------------------------------------------
+static TParams tparams(asg_plan* p) {
+  TParams t;
+  memset(&t, 0, sizeof(t));
+  t.spec = p->spec;
+  t.ncols = p->ncols;
+  t.nT = p->T;
+  t.tw = p->twT;
+  t.twM = p->twM;
+  t.status = p->d_status;
+  t.op.flux = FLUX_NONE;
+  t.op.step = p->d_step;
+  t.op.ncols = p->ncols;
+  t.op.iprev = p->d_iprev;
+  t.op.max_next = p->d_max_next;
+  t.op.pnp = p->o_pnp;
+  t.op.ppp = p->o_ppp;
+  t.op.pI = p->o_pI;
+  t.op.pIloss = p->o_pIloss;
+  t.op.pax = p->o_pax;
+  t.op.pax_col = p->cfg.pax_x * p->Y + p->cfg.pax_y;
+  t.op.max_subcycles = p->cfg.kt_max_subcycles > 0 ? p->cfg.kt_max_subcycles : 1024;
+  t.op.cfl_target = (float)p->cfg.kt_cfl_target;
+  t.op.subcycle_hist = p->d_hist;
+  return t;
+}
+
+static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
+  XYParams x;
+  memset(&x, 0, sizeof(x));
+  x.spec = p->spec;
+  x.X = p->X;
+  x.Y = p->Y;
+  x.G = p->G;
+  x.nplanes = p->F;
+  x.nT = p->T;
+  x.f_of_plane = p->f_of_plane;
+  x.table = table;
+  x.ncx = p->ncx;
+  x.ncy = p->ncy;
+  x.cls_x = p->cls_x;
+  x.cls_y = p->cls_y;
+  x.zero_dc_nyq = zero_dc_nyq;
+  x.twX = p->twX;
+  x.twY = p->twY;
+  x.status = p->d_status;
+  x.status_step = p->d_status_step;
+  x.step = p->d_step;
+  x.max_cur = p->d_max_cur;
+  x.fw_lx = p->fw_lx;
+  x.fw_ly = p->fw_ly;
+  x.fw_exp = p->fw_exp;
+  x.sa_wx = p->sa_wx;
+  x.sa_wy = p->sa_wy;
+  x.sa_coef = p->sa_coef;
+  x.sa_strength = (float)p->cfg.super_absorbing_strength;
+  x.sa_inv2dx = (float)(1.0 / (2.0 * p->cfg.dX));
+  x.sa_invdx = (float)(1.0 / p->cfg.dX);
+  x.sa_inv2dy = (float)(1.0 / (2.0 * p->cfg.dY));
+  x.sa_invdy = (float)(1.0 / p->cfg.dY);
+  x.screen_fscale = p->screen_fscale;
+  x.obl_table = p->obl_tab;
+  x.power_acc = p->power_acc;
+  return x;
+}
+
+static int run_t(asg_plan* p, const TParams& t, int kind = ASG_K_OTHER) {
+  KScope k(p, kind);
+  return asg_launch_t(t, p->tfast, p->gp_t, p->st);
+}
+static int run_xy(asg_plan* p, const XYParams& x, int kind = ASG_K_OTHER) {
+  KScope k(p, kind);
+  return asg_launch_xy(x, p->xyfast, p->gp_x, p->gp_y, p->st);
+}
+
+static void set_flux(asg_plan* p, TParams& t, double dz, double beta_tvd, int flux) {
+  t.op.flux = flux;
+  t.op.dz = (float)dz;
+  t.op.beta_tvd = (float)beta_tvd;
+  t.op.coef_rus = (float)(p->N * dz / p->cfg.dT);
+  t.op.coef_kt = (float)(p->N / p->cfg.dT);
+  t.op.n_rus64 = p->N * dz / p->cfg.dT;
+  t.op.n_kt64 = p->N / p->cfg.dT;
+}
+
+// the nonlinear step of the current stage, with the optional beam-obliquity
+// scaling of N (march_step_*_obl, :923-965)
+static int nonlinear_stage(asg_plan* p, double dz, double beta_tvd, const float* axy,
+                           const float* at) {
+  const int flux = p->cfg.split_step ? p->cfg.flux : ASG_FLUX_RUSANOV;
+  if (!p->cfg.nonlinear_obliquity) {
+    TParams t = tparams(p);
+    t.op.abl_xy = axy;
+    t.op.abl_t = at;
+    set_flux(p, t, dz, beta_tvd, flux);
+    t.do_r2c = 1;
+    return run_t(p, t, ASG_K_T_NONLIN);
+  }
+  // (1) taper only, (2) power sums of the tapered field, (3) flux with N_eff
+  {
+    TParams t = tparams(p);
+    t.op.abl_xy = axy;
+    t.op.abl_t = at;
+    t.do_r2c = 1;
+    CKS(run_t(p, t));
+  }
+  CK(cudaMemsetAsync(p->power_acc, 0, 2 * sizeof(double), p->st));
+  {
+    XYParams x = xyparams(p, nullptr, false);
+    x.power_only = 1;
+    CKS(run_xy(p, x));
+  }
+  TParams t = tparams(p);
+  set_flux(p, t, dz, beta_tvd, flux);
+  t.op.n_scale = p->power_acc;  // ratio formed in the column code
+  t.do_r2c = 1;
+  return run_t(p, t, ASG_K_T_NONLIN);
+}
+
+static int ensure_outputs(asg_plan* p, int cap) {
+  if (p->o_cap >= cap) return ASG_OK;
+  free_outputs(p);
+  const size_t n = (size_t)cap * p->ncols;
+  CKS(dalloc(&p->o_pnp, n));
+  CKS(dalloc(&p->o_ppp, n));
+  CKS(dalloc(&p->o_pI, n));
+  CKS(dalloc(&p->o_pIloss, n));
+  CKS(dalloc(&p->o_pax, (size_t)cap * p->T));
+  p->o_cap = cap;
+  return ASG_OK;
+}
+
+static int status_to_error(asg_plan* p) {
+  unsigned st = 0;
+  int sstep = 0;
+  CK(cudaMemcpy(&st, p->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (st == 0) return ASG_OK;
+  CK(cudaMemcpy(&sstep, p->d_status_step, sizeof(int), cudaMemcpyDeviceToHost));
+  const int code = -(int)st;
+  if (code == ASG_ERR_STABILITY)
+    return fail(code,
+                "stability criterion violated before step %d (N*dZ/dT*max|p| > "
+                "stabilityThreshold); the step cannot shrink below dZmin",
+                sstep);
+  if (code == ASG_ERR_NAN) return fail(code, "non-finite field value before step %d", sstep);
+  return fail(code, "device status %d at step %d", code, sstep);
+}
+
+// one march step; `last` -> write the real field, no forward transform
+static int march_step(asg_plan* p, const Slot& s, double dzs, double btvd, int nscr, int nsrc,
+                      bool last, bool want_real) {
+  const bool split = p->cfg.split_step != 0;
+  const float* axy = split ? p->abl_xy_half : p->abl_xy_full;
+  const float* at = split ? p->abl_t_half : p->abl_t_full;
+  // stage A (+ stability test)
+  {
+    XYParams x = xyparams(p, s.tabA, true);
+    x.check_stability = 1;
+    x.stab_coef = p->N * dzs / p->cfg.dT;
+    x.stab_thr = p->cfg.stability_threshold;
+    CKS(run_xy(p, x, ASG_K_XY_A));
+  }
+  CKS(nonlinear_stage(p, dzs, btvd, axy, at));
+  if (split) {
+    XYParams x = xyparams(p, s.tabB, true);
+    CKS(run_xy(p, x, ASG_K_XY_B));
+    TParams t = tparams(p);
+    t.op.abl_xy = axy;
+    t.op.abl_t = at;
+    t.do_r2c = 1;
+    CKS(run_t(p, t, ASG_K_T_MID));
+  }
+  // closing stage: attenuation + (x, y, omega) epilogue
+  {
+    XYParams x = xyparams(p, s.tabC, false);
+    x.epi = (p->cfg.freq_weighted ? EPI_FREQW : 0) | (p->cfg.super_absorbing ? EPI_SUPERABS : 0);
+    x.nscreens = nscr;
+    x.screens = p->d_screens;
+    CKS(run_xy(p, x, ASG_K_XY_C));
+  }
+  {
+    TParams t = tparams(p);
+    t.stats = 1;
+    t.op.nsrc = nsrc;
+    t.op.src = p->d_src;
+    t.write_real = (last || want_real) ? 1 : 0;
+    t.real_out = p->real;
+    t.do_r2c = last ? 0 : 1;
+    CKS(run_t(p, t, ASG_K_T_END));
+  }
+  KScope k(p, ASG_K_OTHER);
+  return asg_launch_advance(p->d_step, p->d_max_cur, p->d_max_next, p->st);
+}
+
+extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double dz,
+                       asg_step_cb cb, void* user, int* n_steps_out) {
+  g_err.clear();
+  if (!p || !init) return fail(ASG_ERR_ARG, "null argument");
+  if (!p->slot[0].ready) return fail(ASG_ERR_STATE, "asg_set_step_operators(slot 0) not called");
+  if (fabs(p->slot[0].dz - dz) != 0.0)
+    return fail(ASG_ERR_STATE, "slot-0 operators were built for dz=%.17g, run asks %.17g",
+                p->slot[0].dz, dz);
+  // the step sequence, exactly as the reference's while loop forms it
+  std::vector<double> steps;
+  std::vector<double> zbefore;  // sum(zvec) before each step
+  {
+    PySum zs;
+    while (zs.value() < prop_dist - 1e-15) {
+      const double rem = prop_dist - zs.value();
+      const double d = dz < rem ? dz : rem;
+      zbefore.push_back(zs.value());
+      steps.push_back(d);
+      zs.add(d);
+      if (steps.size() > 100000000) return fail(ASG_ERR_ARG, "too many steps");
+    }
+  }
+  const int cap = (int)ceil(prop_dist / dz) + 100;
+  if ((int)steps.size() > cap) return fail(ASG_ERR_ARG, "step count exceeds output capacity");
+  CKS(ensure_outputs(p, cap));
+  // state
+  CK(cudaMemsetAsync(p->d_status, 0, sizeof(unsigned), p->st));
+  CK(cudaMemsetAsync(p->d_step, 0, sizeof(int), p->st));
+  CK(cudaMemsetAsync(p->d_max_cur, 0, sizeof(unsigned), p->st));
+  CK(cudaMemsetAsync(p->d_max_next, 0, sizeof(unsigned), p->st));
+  CK(cudaMemsetAsync(p->d_status_step, 0, sizeof(int), p->st));
+  CK(cudaMemcpyAsync(p->real, init, (size_t)p->ncols * p->T * sizeof(float),
+                     cudaMemcpyHostToDevice, p->st));
+  // initial upload: iprev, stability max, forward transform
+  {
+    TParams t = tparams(p);
+    t.in_real = 1;
+    t.real_in = p->real;
+    t.stats = 1;
+    t.op.init_stats = 1;
+    t.do_r2c = 1;
+    CKS(run_t(p, t));
+    // max_cur <- max_next, step stays 0
+    CKS(asg_launch_advance(p->d_step, p->d_max_cur, p->d_max_next, p->st));
+    CK(cudaMemsetAsync(p->d_step, 0, sizeof(int), p->st));
+  }
+  p->zaxis.clear();
+  for (int i = 0; i < ASG_NKINDS; ++i) {
+    p->launches[i] = 0;
+    p->kms[i] = 0.0;
+  }
+  p->ev_kind.clear();
+  CK(cudaEventRecord(p->ev0, p->st));
+  double zcum = 0.0;  // np.cumsum(zvec): plain sequential sum (:1562)
+  PySum zsum;
+  std::vector<ScreenDev> scr;
+  std::vector<SourceEvent> src;
+  for (size_t k = 0; k < steps.size(); ++k) {
+    const double dzs = steps[k];
+    const double z = zbefore[k];
+    const bool partial = fabs(dzs - dz) > 1e-15;
+    const Slot* s = &p->slot[0];
+    if (partial) {
+      if (!p->slot[1].ready || p->slot[1].dz != dzs)
+        return fail(ASG_ERR_STATE, "partial step dz=%.17g needs asg_set_step_operators(slot 1)",
+                    dzs);
+      s = &p->slot[1];
+    }
+    scr.clear();
+    for (auto& sc : p->screens)
+      if (z < sc.z && sc.z <= z + dzs) scr.push_back(ScreenDev{sc.phase, sc.amp});
+    src.clear();
+    for (auto& so : p->sources)
+      if (z < so.z && so.z <= z + dzs) src.push_back(SourceEvent{so.map, so.val});
+    if (scr.size() > 64 || src.size() > 64)
+      return fail(ASG_ERR_ARG, "more than 64 screens or sources in one step");
+    if (!scr.empty()) CKS(h2d(p->d_screens, scr.data(), scr.size(), p->st));
+    if (!src.empty()) CKS(h2d(p->d_src, src.data(), src.size(), p->st));
+    const bool last = (k + 1 == steps.size());
+    const double norm_step = dzs / (p->cfg.c0 / p->cfg.f0);
+    const double btvd = fmax(1.0, 2.0 - p->cfg.adaptive_filter_strength * norm_step * 10);
+    CKS(march_step(p, *s, dzs, btvd, (int)scr.size(), (int)src.size(), last, cb != nullptr));
+    zcum += dzs;
+    zsum.add(dzs);
+    p->zaxis.push_back(zcum);
+    if (cb) {
+      CK(cudaStreamSynchronize(p->st));
+      CKS(status_to_error(p));
+      cb(user, (int)k, zsum.value(), p->real);
+    }
+  }
+  CK(cudaEventRecord(p->ev1, p->st));
+  CK(cudaStreamSynchronize(p->st));
+  collect_kernel_times(p);
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, p->ev0, p->ev1));
+  p->run_ms = ms;
+  p->nsteps = (int)steps.size();
+  if (n_steps_out) *n_steps_out = p->nsteps;
+  return status_to_error(p);
+}
+
+extern "C" int asg_get_outputs(asg_plan* p, float* field, float* pnp, float* ppp, float* pI,
+                               float* pIloss, double* zaxis, float* pax) {
+  g_err.clear();
+  if (!p) return fail(ASG_ERR_ARG, "null plan");
+  const int nz = p->nsteps;
+  const size_t nc = p->ncols;
+  if (field)
+    CK(cudaMemcpy(field, p->real, nc * p->T * sizeof(float), cudaMemcpyDeviceToHost));
+  if (nz > 0) {
+    float* tmp = nullptr;
+    CKS(dalloc(&tmp, (size_t)nz * (nc > (size_t)p->T ? nc : (size_t)p->T)));
+    float* srcs[4] = {p->o_pnp, p->o_ppp, p->o_pI, p->o_pIloss};
+    float* dsts[4] = {pnp, ppp, pI, pIloss};
+    for (int i = 0; i < 4; ++i) {
+      if (!dsts[i]) continue;
+      CKS(asg_launch_transpose(srcs[i], tmp, nz, (int)nc, p->st));
+      CK(cudaMemcpyAsync(dsts[i], tmp, (size_t)nz * nc * sizeof(float), cudaMemcpyDeviceToHost,
+                         p->st));
+      CK(cudaStreamSynchronize(p->st));
+    }
+    if (pax) {
+      CKS(asg_launch_transpose(p->o_pax, tmp, nz, p->T, p->st));
+      CK(cudaMemcpyAsync(pax, tmp, (size_t)nz * p->T * sizeof(float), cudaMemcpyDeviceToHost,
+                         p->st));
+      CK(cudaStreamSynchronize(p->st));
+    }
+    cudaFree(tmp);
+  }
+  if (zaxis && nz > 0) memcpy(zaxis, p->zaxis.data(), nz * sizeof(double));
+  return ASG_OK;
+}
+
+extern "C" int asg_set_profiling(asg_plan* p, int enable) {
+  if (!p) return fail(ASG_ERR_ARG, "null plan");
+  p->prof = enable != 0;
+  return ASG_OK;
+}
+
+extern "C" int asg_kernel_stats(asg_plan* p, double* ms, long* launches, int nkinds) {
+  if (!p || nkinds <= 0) return fail(ASG_ERR_ARG, "bad argument");
+  for (int i = 0; i < nkinds && i < ASG_NKINDS; ++i) {
+    if (ms) ms[i] = p->kms[i];
+    if (launches) launches[i] = p->launches[i];
+  }
+  return ASG_OK;
+}
+
+extern "C" int asg_last_run_ms(asg_plan* p, double* ms) {
+  if (!p || !ms) return fail(ASG_ERR_ARG, "null argument");
+  *ms = p->run_ms;
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single operators on a host field (parity tests of each stage)
+// ---------------------------------------------------------------------------
+extern "C" int asg_apply_operator(asg_plan* p, int op, float* field, int screen_index,
+                                  double* scalar_out) {
+  g_err.clear();
+  if (!p || !field) return fail(ASG_ERR_ARG, "null argument");
+  if (!p->slot[0].ready) return fail(ASG_ERR_STATE, "operators not set");
+  Slot& s = p->slot[0];
+  const size_t n = (size_t)p->ncols * p->T;
+  CK(cudaMemsetAsync(p->d_status, 0, sizeof(unsigned), p->st));
+  CK(cudaMemsetAsync(p->d_step, 0, sizeof(int), p->st));
+  CK(cudaMemcpyAsync(p->real, field, n * sizeof(float), cudaMemcpyHostToDevice, p->st));
+  {
+    TParams t = tparams(p);
+    t.in_real = 1;
+    t.real_in = p->real;
+    t.do_r2c = 1;
+    CKS(run_t(p, t));
+  }
+  const float* axy = nullptr;
+  const float* at = nullptr;
+  XYParams x = xyparams(p, nullptr, false);
+  switch (op) {
+    case 1:
+    case 2:
+      CKS(build_table(p, s, p->tab_scratch, true, op == 1 ? s.dz : s.dz / 2, false, 0.0));
+      x.table = p->tab_scratch;
+      x.zero_dc_nyq = 1;
+      axy = op == 1 ? p->abl_xy_full : p->abl_xy_half;
+      at = op == 1 ? p->abl_t_full : p->abl_t_half;
+      break;
+    case 3:
+    case 4:
+      CKS(build_table(p, s, p->tab_scratch, false, 0.0, true, op == 3 ? s.dz : s.dz * 0.5));
+      x.table = p->tab_scratch;
+      x.epi = 0;
+      break;
+    case 5: x.epi = EPI_FREQW; break;
+    case 6: x.epi = EPI_SUPERABS; break;
+    case 7: {
+      if (screen_index < 0 || screen_index >= (int)p->screens.size())
+        return fail(ASG_ERR_ARG, "screen index %d out of range", screen_index);
+      ScreenDev sd{p->screens[screen_index].phase, p->screens[screen_index].amp};
+      CKS(h2d(p->d_screens, &sd, 1, p->st));
+      x.nscreens = 1;
+      x.screens = p->d_screens;
+      break;
+    }
+    case 8: {
+      if (!p->obl_tab) return fail(ASG_ERR_STATE, "plan built without nonlinear obliquity");
+      CK(cudaMemsetAsync(p->power_acc, 0, 2 * sizeof(double), p->st));
+      x.power_only = 1;
+      CKS(run_xy(p, x));
+      double acc[2];
+      CK(cudaMemcpyAsync(acc, p->power_acc, sizeof(acc), cudaMemcpyDeviceToHost, p->st));
+      CK(cudaStreamSynchronize(p->st));
+      if (scalar_out) *scalar_out = acc[0] / (acc[1] + 1e-30);
+      return status_to_error(p);
+    }
+    default: return fail(ASG_ERR_ARG, "unknown operator %d", op);
+  }
+  CKS(run_xy(p, x));
+  {
+    TParams t = tparams(p);
+    t.op.abl_xy = axy;
+    t.op.abl_t = at;
+    t.write_real = 1;
+    t.real_out = p->real;
+    t.do_r2c = 0;
+    CKS(run_t(p, t));
+  }
+  CK(cudaMemcpyAsync(field, p->real, n * sizeof(float), cudaMemcpyDeviceToHost, p->st));
+  CK(cudaStreamSynchronize(p->st));
+  return status_to_error(p);
+}
+
+extern "C" int asg_flux_columns(const float* in, float* out, int ncols, int nT, int flux,
+                                double n_coef, double dz, double dt, double beta_tvd,
+                                double cfl_target, int max_subcycles) {
+  g_err.clear();
+  if (!in || !out || ncols <= 0 || nT < 3) return fail(ASG_ERR_ARG, "bad argument");
+  if ((nT + 31) / 32 > 64 || asg_t_generic_smem(nT) > 200 * 1024)
+    return fail(ASG_ERR_SHAPE, "nT=%d too long", nT);
+  if (flux < ASG_FLUX_RUSANOV || flux > ASG_FLUX_KT_MINMOD)
+    return fail(ASG_ERR_ARG, "unknown flux %d", flux);
+  CKS(upload_roots());
+  float *d = nullptr, *dout = nullptr;
+  unsigned* st = nullptr;
+  float2* tw = nullptr;
+  const size_t n = (size_t)ncols * nT;
+  CKS(dalloc(&d, n));
+  CKS(dalloc(&dout, n));
+  CKS(dalloc(&st, 1));
+  CKS(dalloc(&tw, nT));
+  CK(cudaMemset(st, 0, sizeof(unsigned)));
+  CK(cudaMemcpy(d, in, n * sizeof(float), cudaMemcpyHostToDevice));
+  TParams t;
+  memset(&t, 0, sizeof(t));
+  t.ncols = ncols;
+  t.nT = nT;
+  t.in_real = 1;
+  t.real_in = d;
+  t.write_real = 1;
+  t.real_out = dout;
+  t.tw = tw;
+  t.status = st;
+  t.op.flux = flux;
+  t.op.dz = (float)dz;
+  t.op.beta_tvd = (float)beta_tvd;
+  t.op.coef_rus = (float)(n_coef * dz / dt);
+  t.op.coef_kt = (float)(n_coef / dt);
+  t.op.n_rus64 = n_coef * dz / dt;
+  t.op.n_kt64 = n_coef / dt;
+  t.op.cfl_target = (float)cfl_target;
+  t.op.max_subcycles = max_subcycles > 0 ? max_subcycles : 1024;
+  GenPlan gp = make_gen_plan(nT);
+  int s = asg_launch_t(t, false, gp, 0);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (s == ASG_OK && e == cudaSuccess)
+    e = cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(dout);
+  cudaFree(st);
+  cudaFree(tw);
+  if (s != ASG_OK) return fail(s, "flux kernel launch failed");
+  if (e != cudaSuccess) return fail(ASG_ERR_CUDA, "%s", cudaGetErrorString(e));
+  return ASG_OK;
+}
+
+extern "C" const char* asg_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* asg_version(void) {
+  return "asg_gb300 1 (sm_103a; fast t sizes 128..2048, fast xy nY 64..512 with nX = 32*G)";
+}

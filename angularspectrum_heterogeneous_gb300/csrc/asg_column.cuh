@@ -1,0 +1,354 @@
+// Per-(x,y)-column work along t, executed by one warp per column on a
+// column held in shared memory: boundary taper, Burgers step (Rusanov,
+// TVD-Rusanov, KT-MC, KT-minmod; SSP-RK2; optional per-column CFL
+// sub-cycling), source-plane injection and the per-step accumulators.
+//
+// Reference semantics (angular_spectrum_solver.py):
+//   taper                 :125-129, :655   (u * abl, separable x*y*t)
+//   _rusanov_flux_standard :688-696
+//   _rusanov_flux_tvd      :699-724
+//   _kt_rhs/_kt_rhs_minmod :758-830,  _kt_flux/_kt_flux_minmod :833-868
+//   _kt_flux_adaptive      :842-859  (here per column, see below)
+//   source injection      :1521-1527
+//   accumulators          :1445, :1529-1535
+#pragma once
+#include "asg_common.cuh"
+
+enum FluxKind : int {
+  FLUX_NONE = 0,
+  FLUX_RUSANOV = 1,      // _rusanov_flux_standard
+  FLUX_RUSANOV_TVD = 2,  // _rusanov_flux_tvd
+  FLUX_KT_MC = 3,        // _kt_flux
+  FLUX_KT_MINMOD = 4,    // _kt_flux_minmod
+};
+
+struct SourceEvent {
+  const int* map;     // [ncols] -> row in val, or -1
+  const float* val;   // [nactive][nT]
+};
+
+// Everything the column phase needs (plain POD, passed by value inside the
+// kernel parameter block).
+struct ColumnOps {
+  // taper: u *= abl_xy[c] * abl_t[t]   (null abl_xy -> no taper)
+  const float* abl_xy;
+  const float* abl_t;
+  // Burgers
+  int flux;
+  // coefficients rounded once from FP64 on the host, as the reference's
+  // float32 arrays see its float64 scalars: coef_rus = N dZ/dT, coef_kt = N/dT
+  float coef_rus, coef_kt;
+  const double* n_scale; // optional device pair (sum P k/kz, sum P) for <k/kz>, or null
+  double n_rus64, n_kt64;  // the same coefficients in FP64 (used with n_scale)
+  float dz, beta_tvd;
+  float cfl_target;      // > 0: per-column sub-cycling for the KT schemes
+  int max_subcycles;     // bound on the per-column sub-cycle count
+  // sources (step end)
+  int nsrc;
+  const SourceEvent* src;
+  // accumulators (step end); step index read from *step
+  int accumulate;
+  const int* step;
+  float *pnp, *ppp, *pI, *pIloss;  // [step][ncols]
+  float* pax;                       // [step][nT]
+  int pax_col;
+  int ncols;
+  double* iprev;                    // [ncols]
+  unsigned* max_next;               // stability max of the field entering the next step
+  unsigned* subcycle_hist;          // optional [64] histogram of per-column sub-cycles
+  int init_stats;                   // first upload: only iprev / max_next
+};
+
+// Column accessor over shared memory: real samples t = 0..nT-1.
+// Fast layout: complex slots with one pad every N2 slots (LinePlan::pos).
+template <int N2>
+struct PaddedColumn {
+  float* base;
+  ASG_DEV int idx(int t) const { int j = t >> 1; return 2 * (j + j / N2) + (t & 1); }
+  ASG_DEV float get(int t) const { return base[idx(t)]; }
+  ASG_DEV void set(int t, float v) const { base[idx(t)] = v; }
+};
+struct PlainColumn {
+  float* base;
+  ASG_DEV float get(int t) const { return base[t]; }
+  ASG_DEV void set(int t, float v) const { base[t] = v; }
+};
+
+// ---------------------------------------------------------------------------
+// flux primitives (float32, same formulas and order as the reference)
+// ---------------------------------------------------------------------------
+ASG_DEV float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+
+// interface flux of _rusanov_flux_standard (:691-694)
+ASG_DEV float rus_std_fh(float uL, float uR) {
+  float a = fmaxf(fabsf(uL), fabsf(uR));
+  return -(uL * uL + uR * uR) / 2.f - a * (uR - uL);
+}
+// interface flux of _rusanov_flux_tvd (:702-705)
+ASG_DEV float rus_tvd_fh(float uL, float uR) {
+  float a = fmaxf(fabsf(uL), fabsf(uR));
+  return 0.5f * (-0.5f * (uL * uL + uR * uR)) - 0.5f * a * (uR - uL);
+}
+ASG_DEV float tvd_phi(float r, float b) {
+  return fmaxf(0.f, fminf(fminf(b * r, 1.f), fminf(r, b)));
+}
+ASG_DEV float minmod2(float a, float b) {
+  return (a * b > 0.f) ? sgnf(a) * fminf(fabsf(a), fabsf(b)) : 0.f;
+}
+ASG_DEV float minmod3(float a, float b, float c) {
+  bool ok = (a * b > 0.f) && (b * c > 0.f);
+  return ok ? sgnf(a) * fminf(fminf(fabsf(a), fabsf(b)), fabsf(c)) : 0.f;
+}
+// limited slope at a cell given its left/right neighbours (MC or minmod)
+template <bool MC>
+ASG_DEV float kt_slope(float um1, float u0, float up1) {
+  float dm = u0 - um1, dp = up1 - u0;
+  return MC ? minmod3(2.f * dm, 0.5f * (dm + dp), 2.f * dp) : minmod2(dm, dp);
+}
+// KT interface flux from the reconstructed states (:772-793)
+ASG_DEV float kt_fh(float um, float up) {
+  float ap = fmaxf(fmaxf(-um, -up), 0.f);
+  float am = fminf(fminf(-um, -up), 0.f);
+  float fm = -0.5f * um * um;
+  float fp = -0.5f * up * up;
+  float den = ap - am;
+  bool small = fabsf(den) < 1e-14f;
+  if (small) {
+    return 0.5f * (fm + fp) - 0.5f * fmaxf(fabsf(um), fabsf(up)) * (up - um);
+  }
+  return (ap * fm - am * fp - ap * am * (up - um)) / den;
+}
+
+// ---------------------------------------------------------------------------
+// Burgers step on one column by one warp.  Each lane owns a contiguous chunk
+// [t0, t1) of the column; the stencil halo is read from shared memory.  The
+// column end points t=0 and t=nT-1 are never updated (zero boundary rhs).
+// ---------------------------------------------------------------------------
+template <int CH, class Col>
+ASG_DEV void rusanov_column(const Col& col, int nT, float coef, bool tvd, float beta_tvd,
+                            unsigned mask) {
+  const int lane = threadIdx.x & 31;
+  const int t0 = lane * CH;
+  float out[CH];
+  // original values in a window [t0-1, t0+CH]
+  float w[CH + 2];
+#pragma unroll
+  for (int i = 0; i < CH + 2; ++i) {
+    int t = t0 - 1 + i;
+    w[i] = (t >= 0 && t < nT) ? col.get(t) : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    float u = w[i + 1];
+    out[i] = u;
+    if (t >= 1 && t < nT - 1) {
+      float um = w[i], up = w[i + 2];
+      if (!tvd) {
+        float fd = rus_std_fh(u, up) - rus_std_fh(um, u);
+        out[i] = u + (-coef * fd);
+      } else {
+        float fd = rus_tvd_fh(u, up) - rus_tvd_fh(um, u);
+        float dm = u - um, dp = up - u;
+        const float eps = 1e-30f;
+        float r = dp / (dm + eps * sgnf(dm + eps));
+        float ri = dm / (dp + eps * sgnf(dp + eps));
+        float lim = 0.5f * (tvd_phi(r, beta_tvd) + tvd_phi(ri, beta_tvd)) * fd;
+        out[i] = u + (-coef * lim);
+      }
+    }
+  }
+  __syncwarp(mask);
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    if (t < nT) col.set(t, out[i]);
+  }
+  __syncwarp(mask);
+}
+
+// rhs of the KT scheme at the lane's CH points from a window of CH+4 values
+template <int CH, bool MC>
+ASG_DEV void kt_rhs_window(const float (&w)[CH + 4], int t0, int nT, float ndt, float (&rhs)[CH]) {
+  // slopes at window positions 1..CH+2  (t0-1 .. t0+CH); zero at the column ends
+  float s[CH + 2];
+#pragma unroll
+  for (int i = 0; i < CH + 2; ++i) {
+    int t = t0 - 1 + i;
+    s[i] = (t >= 1 && t < nT - 1) ? kt_slope<MC>(w[i], w[i + 1], w[i + 2]) : 0.f;
+  }
+  // interface fluxes at t+1/2 for t = t0-1 .. t0+CH-1
+  float fh[CH + 1];
+#pragma unroll
+  for (int i = 0; i < CH + 1; ++i) {
+    float um = w[i + 1] + 0.5f * s[i];
+    float up = w[i + 2] - 0.5f * s[i + 1];
+    fh[i] = kt_fh(um, up);
+  }
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    rhs[i] = (t >= 1 && t < nT - 1) ? (-ndt * (fh[i + 1] - fh[i])) : 0.f;
+  }
+}
+
+template <int CH, bool MC, class Col>
+ASG_DEV void load_window4(const Col& col, int t0, int nT, float (&w)[CH + 4]) {
+#pragma unroll
+  for (int i = 0; i < CH + 4; ++i) {
+    int t = t0 - 2 + i;
+    w[i] = (t >= 0 && t < nT) ? col.get(t) : 0.f;
+  }
+}
+
+// one SSP-RK2 KT step of size dz on the column
+template <int CH, bool MC, class Col>
+ASG_DEV void kt_column_step(const Col& col, int nT, float ndt, float dz, unsigned mask) {
+  const int lane = threadIdx.x & 31;
+  const int t0 = lane * CH;
+  float w[CH + 4];
+  load_window4<CH, MC>(col, t0, nT, w);
+  float u[CH], rhs[CH];
+#pragma unroll
+  for (int i = 0; i < CH; ++i) u[i] = w[i + 2];
+  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
+  __syncwarp(mask);
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    if (t < nT) col.set(t, u[i] + dz * rhs[i]);  // stage1
+  }
+  __syncwarp(mask);
+  load_window4<CH, MC>(col, t0, nT, w);
+  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
+  __syncwarp(mask);
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    float s1 = w[i + 2];
+    if (t < nT) col.set(t, 0.5f * u[i] + 0.5f * (s1 + dz * rhs[i]));
+  }
+  __syncwarp(mask);
+}
+
+template <int CH, class Col>
+ASG_DEV float column_absmax(const Col& col, int nT) {
+  const int lane = threadIdx.x & 31;
+  float m = 0.f;
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = lane * CH + i;
+    if (t < nT) m = fmaxf(m, fabsf(col.get(t)));
+  }
+  return warp_max(m);
+}
+
+// ---------------------------------------------------------------------------
+// The whole column phase.  CH = ceil(nT/32) samples per lane.
+// ---------------------------------------------------------------------------
+template <int CH, class Col>
+ASG_DEV float column_phase(const Col& col, int c, int nT, const ColumnOps& op, bool write_stats) {
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = 0xffffffffu;
+  // 1) taper
+  if (op.abl_xy != nullptr) {
+    const float axy = op.abl_xy[c];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      int t = lane + 32 * i;
+      if (t < nT) col.set(t, col.get(t) * (axy * op.abl_t[t]));
+    }
+    __syncwarp(mask);
+  }
+  // 2) Burgers
+  if (op.flux != FLUX_NONE) {
+    float coef_rus = op.coef_rus, ndt = op.coef_kt;
+    if (op.n_scale != nullptr) {
+      // n_scale = {sum P k/kz, sum P over propagating modes}: <k/kz> (:641-643)
+      const double sc = op.n_scale[0] / (op.n_scale[1] + 1e-30);
+      coef_rus = (float)(op.n_rus64 * sc);
+      ndt = (float)(op.n_kt64 * sc);
+    }
+    if (op.flux == FLUX_RUSANOV || op.flux == FLUX_RUSANOV_TVD) {
+      rusanov_column<CH>(col, nT, coef_rus, op.flux == FLUX_RUSANOV_TVD, op.beta_tvd, mask);
+    } else {
+      int nsub = 1;
+      if (op.cfl_target > 0.f) {
+        float um = column_absmax<CH>(col, nT);
+        float cfl = ndt * um * op.dz;
+        if (!(cfl <= op.cfl_target || um < 1e-30f)) {
+          float q = ceilf(cfl / op.cfl_target);
+          nsub = (q > (float)op.max_subcycles) ? op.max_subcycles : (int)q;
+        }
+        if (op.subcycle_hist != nullptr && lane == 0)
+          atomicAdd(op.subcycle_hist + min(nsub, 63), 1u);
+      }
+      float dzs = op.dz / (float)nsub;
+      for (int k = 0; k < nsub; ++k) {
+        if (op.flux == FLUX_KT_MC) kt_column_step<CH, true>(col, nT, ndt, dzs, mask);
+        else kt_column_step<CH, false>(col, nT, ndt, dzs, mask);
+      }
+    }
+  }
+  // 3) sources, in list order
+  for (int e = 0; e < op.nsrc; ++e) {
+    int row = op.src[e].map[c];
+    if (row >= 0) {
+      const float* v = op.src[e].val + (size_t)row * nT;
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        int t = lane + 32 * i;
+        if (t < nT) col.set(t, col.get(t) + v[t]);
+      }
+    }
+    __syncwarp(mask);
+  }
+  // 4) accumulators (pI/pIloss sums in FP64 across lanes); returns max|u|
+  //    (NaN/inf if the column holds a non-finite value) for the stability test
+  float am = 0.f;
+  if (write_stats) {
+    float s = 0.f, mn = INFINITY, mx = -INFINITY;
+    double sd = 0.0;
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+      int t = lane + 32 * i;
+      if (t < nT) {
+        float u = col.get(t);
+        s = fmaf(u, u, s);
+        mn = fminf(mn, u);
+        mx = fmaxf(mx, u);
+        am = fmaxf(am, fabsf(u));
+        bad |= !(fabsf(u) <= 3.402823466e38f);
+        if ((i & 7) == 7) { sd += (double)s; s = 0.f; }
+      }
+    }
+    sd += (double)s;
+    sd = warp_sum(sd);
+    mn = warp_min(mn);
+    mx = warp_max(mx);
+    am = warp_max(am);
+    bad = __any_sync(mask, bad);
+    if (bad) am = __uint_as_float(0x7fc00000u);
+    if (lane == 0) {
+      if (!op.init_stats) {
+        const size_t o = (size_t)(*op.step) * (size_t)op.ncols + (size_t)c;
+        const double ib = op.iprev[c];
+        op.pIloss[o] = (float)fmax(0.0, ib - sd);
+        op.pI[o] = (float)sd;
+        op.pnp[o] = mn;
+        op.ppp[o] = mx;
+      }
+      op.iprev[c] = sd;
+    }
+    if (c == op.pax_col && !op.init_stats) {
+      float* pa = op.pax + (size_t)(*op.step) * (size_t)nT;
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        int t = lane + 32 * i;
+        if (t < nT) pa[t] = col.get(t);
+      }
+    }
+  }
+  return am;
+}

@@ -1,0 +1,118 @@
+// Internal declarations shared by the kernel translation units and the
+// C-ABI layer.  Not part of the public interface (see include/asg_gb300.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "asg_gb300.h"
+
+struct SourceEvent;
+struct GenPlan;
+
+// ---- t-column pass ---------------------------------------------------------
+#include "asg_column.cuh"
+
+struct TParams {
+  float2* spec;          // [planes][ncols]
+  int ncols, nT;
+  int in_real;           // read real columns from real_in instead of the spectrum
+  const float* real_in;  // [ncols][nT]
+  int write_real;        // write the real column to real_out after the column phase
+  float* real_out;
+  int do_r2c;            // write the spectrum back
+  int stats;             // accumulators / stability max in the column phase
+  ColumnOps op;
+  const float2* tw;      // W_nT^k, k < nT
+  const float2* twM;     // W_M^k,  k < M (fast kernels)
+  const unsigned* status;
+};
+
+bool asg_t_fast_supported(int nT);
+size_t asg_t_generic_smem(int nT);
+int asg_launch_t(const TParams& p, bool fast, const GenPlan& pl, cudaStream_t st);
+
+// ---- xy-plane pass ---------------------------------------------------------
+struct ScreenDev {
+  const float* phase;    // [X][Y]
+  const float* amp;      // [X][Y] or null
+};
+
+enum EpiFlags : int {
+  EPI_FREQW = 1,         // frequency-weighted boundary
+  EPI_SUPERABS = 2,      // Engquist-Majda super-absorbing boundary
+};
+
+struct XYParams {
+  float2* spec;          // [planes][X][Y]
+  int X, Y, G;           // G CTAs per plane (thread-block cluster), R = X / G rows each
+  int nplanes;
+  int nT;
+  const int* f_of_plane; // rfft bin held by each plane
+  const float2* table;   // [plane][ncx][ncy] multiplier (normalisation folded in) or null
+  int ncx, ncy;
+  const int* cls_x;      // [X] multiplier class of each x slot
+  const int* cls_y;      // [Y] multiplier class of each y slot
+  int zero_dc_nyq;       // planes of bin 0 and nT/2 are zeroed (analytic-signal propagator)
+  const float2* twX;     // W_X^k
+  const float2* twY;     // W_Y^k
+  // power-spectrum reduction (nonlinear obliquity); forward transform only
+  int power_only;
+  const float* obl_table;  // [plane][ncx][ncy] k/kz (0 = excluded)
+  double* power_acc;       // [2] sum P*obl, sum P*mask
+  // stability test at the start of a step
+  int check_stability;
+  const unsigned* max_cur;
+  double stab_coef;        // N dZ_step / dT
+  double stab_thr;
+  // epilogue in (x, y, omega): stage closing a step
+  int epi;
+  const float* fw_lx;      // log2 taper along x [X]   (freq-weighted)
+  const float* fw_ly;      // log2 taper along y [Y]
+  const float* fw_exp;     // exponent per plane
+  const float* sa_wx;      // boundary weights [X]       (super-absorbing)
+  const float* sa_wy;      // [Y]
+  const float* sa_coef;    // per plane: c0/omega (0 where excluded); coeff = -i*sa_coef
+  float sa_strength;
+  float sa_inv2dx, sa_invdx, sa_inv2dy, sa_invdy;
+  int nscreens;
+  const ScreenDev* screens;
+  const float* screen_fscale;  // per plane: f / max(f0_bin, 1)
+  unsigned* status;
+  int* status_step;
+  const int* step;
+};
+
+bool asg_xy_fast_supported(int X, int Y, int* G_out);
+size_t asg_xy_generic_smem(int X, int Y);
+int asg_launch_xy(const XYParams& p, bool fast, const GenPlan& plx, const GenPlan& ply,
+                  cudaStream_t st);
+
+// ---- set-up kernels (FP64) -------------------------------------------------
+struct TableParams {
+  int nplanes, ncx, ncy;
+  const double* kx2;       // [ncx] kx^2 of each class
+  const double* ky2;       // [ncy]
+  const double* kt_prop;   // [plane] propagator temporal wavenumber (shifted centred grid)
+  const double* km_att;    // [plane] 2 pi f / (nT dT c0)
+  const double* alpha;     // [plane] alpha(f)
+  const double* astar;     // [plane] alphaStar(f)
+  const int* f_of_plane;
+  int nT;
+  double dz_prop;          // dZ or dZ/2
+  double dz_att;           // dZ * scale
+  double kstart, kmax_t;   // cosine k-filter band
+  int use_prop, use_att, obliquity, clip_negative;
+  double norm;             // 1/(X*Y) folded in
+  float2* out;
+};
+int asg_launch_table(const TableParams& p, cudaStream_t st);
+int asg_launch_obl_table(const TableParams& p, float* out, cudaStream_t st);
+
+// device-side bookkeeping between steps
+int asg_launch_advance(int* step, unsigned* max_cur, unsigned* max_next, cudaStream_t st);
+// (x,y,nZ) <- [nZ][x*y] transposes for the outputs
+int asg_launch_transpose(const float* in, float* out, int nz, int ncols, cudaStream_t st);
+
+int asg_roots_upload_t(const float2* w192, const float2* w64);
+int asg_roots_upload_xy(const float2* w192, const float2* w64);

@@ -1,0 +1,281 @@
+"""Drop-in solver API: ``SolverParams`` and ``angular_spectrum_solve``.
+
+Same names, fields, defaults, arguments and return tuple as the reference
+(``angular_spectrum_solver.py:35-76`` and ``:1217-1567``); the march itself
+runs on the GPU through the C ABI of ``libasgb300.so``.
+
+Differences from the reference, all deliberate:
+
+* When the stability test fails (``:1420``), the reference restarts from z=0
+  with a step that can never fall below ``dZmin`` and so never terminates;
+  here :class:`StabilityError` is raised.
+* A non-finite field raises ``ASGError(ASG_ERR_NAN)``; the reference carries
+  NaNs along silently.
+* ``per_step_callback`` receives a torch CUDA tensor *view* of the field
+  (valid during the call; clone it to keep it) where the reference passes a
+  JAX array.
+* Time-of-flight extraction needs the ``tof_extraction`` module, which is not
+  part of the reference tree; asking for it raises ``NotImplementedError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time as _time
+from dataclasses import dataclass
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import ASGError, StabilityError  # noqa: F401  (re-exported)
+from .operators import step_operators, step_sequence
+
+
+@dataclass
+class SolverParams:
+    """All solver parameters (defaults as in the reference, ``:35-76``)."""
+    dX: float = 0.0
+    dY: float = 0.0
+    dT: float = 0.0
+    c0: float = 1500.0
+    rho0: float = 1000.0
+    beta: float = 3.5
+    alpha0: float = 0.5          # dB/MHz^pow/cm  (negative -> water)
+    attenPow: float = 1.0
+    f0: float = 5e6
+    propDist: float = 0.08
+    boundaryFactor: float = 0.2
+    useSplitStep: bool = True
+    useAdaptiveFiltering: bool = True
+    useTVD: bool = True
+    freqFilterThreshold: float = 0.05
+    adaptiveFilterStrength: float = 0.7
+    stabilityThreshold: float = 0.2
+    stabilityRecoveryFactor: float = 0.15
+    dZmin: float = 1e-3
+    useBoundaryLayer: bool = True
+    boundaryProfile: str = 'quadratic'
+    useFreqWeightedBoundary: bool = False
+    useSuperAbsorbing: bool = False
+    superAbsorbingStrength: float = 0.8
+    fluxScheme: str = 'rusanov'
+    useObliquityCorrection: bool = True
+    useNonlinearityObliquity: bool = False
+    phaseScreens: object = None
+    sourcePlanes: object = None
+
+
+def flux_kind(params) -> int:
+    """Nonlinear scheme the driver dispatches to (``:1454-1492``): Lie always
+    uses the standard Rusanov flux; Strang uses KT, TVD-Rusanov or Rusanov."""
+    if not params.useSplitStep:
+        return _lib.FLUX_RUSANOV
+    if params.fluxScheme == 'kt':
+        return _lib.FLUX_KT
+    if params.useTVD:
+        return _lib.FLUX_RUSANOV_TVD
+    return _lib.FLUX_RUSANOV
+
+
+def initial_step(initial_field, params) -> float:
+    """dZ of the reference (``:1292-1296``); it always equals dZmin."""
+    N = params.beta / (2 * params.c0 ** 3 * params.rho0)
+    max_amp = float(np.max(np.abs(initial_field)))
+    dz = min(params.stabilityRecoveryFactor * params.dT / (max_amp * N + 1e-30),
+             params.dZmin) if max_amp > 0 else params.dZmin
+    return max(dz, params.dZmin)
+
+
+class Plan:
+    """One GPU plan: grid, options, operators, screens and sources."""
+
+    def __init__(self, shape, params, kt_cfl_target: float = 0.0, kt_max_subcycles: int = 64):
+        self.lib = _lib.load()
+        nX, nY, nT = shape
+        self.shape = (nX, nY, nT)
+        self.params = params
+        cfg = _lib.Config()
+        cfg.nX, cfg.nY, cfg.nT = nX, nY, nT
+        cfg.dX, cfg.dY, cfg.dT = params.dX, params.dY, params.dT
+        cfg.c0, cfg.rho0, cfg.beta, cfg.f0 = params.c0, params.rho0, params.beta, params.f0
+        cfg.split_step = int(bool(params.useSplitStep))
+        cfg.flux = flux_kind(params)
+        cfg.boundary_layer = int(bool(params.useBoundaryLayer))
+        cfg.freq_weighted = int(bool(params.useFreqWeightedBoundary))
+        cfg.super_absorbing = int(bool(params.useSuperAbsorbing))
+        cfg.super_absorbing_strength = params.superAbsorbingStrength
+        cfg.nonlinear_obliquity = int(bool(params.useNonlinearityObliquity))
+        cfg.stability_threshold = params.stabilityThreshold
+        cfg.adaptive_filter_strength = params.adaptiveFilterStrength
+        cfg.kt_cfl_target = kt_cfl_target
+        cfg.kt_max_subcycles = kt_max_subcycles
+        cfg.pax_x, cfg.pax_y = nX // 2, nY // 2
+        h = C.c_void_p()
+        _lib.check(self.lib.asg_plan_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = []
+        self.n_screens = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asg_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_operators(self, slot: int, dz: float):
+        nX, nY, nT = self.shape
+        o = step_operators(self.params, nX, nY, nT, dz)
+        arrs = {}
+
+        def d(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            arrs[id(a)] = a
+            return _lib.dptr(a)
+
+        s = _lib.StepOps()
+        s.dz = dz
+        s.kx, s.ky, s.kt = d(o.kx), d(o.ky), d(o.kt)
+        s.kfilt_start, s.kfilt_max = o.kfilt_start, o.kfilt_max
+        s.alpha, s.alpha_star = d(o.alpha), d(o.alpha_star)
+        s.atten_obliquity = int(o.atten_obliquity)
+        s.atten_clip_negative = int(o.atten_clip_negative)
+        s.abl_x, s.abl_y, s.abl_t = d(o.abl_x), d(o.abl_y), d(o.abl_t)
+        s.fw_exponent, s.fw_taper_x, s.fw_taper_y = d(o.fw_exponent), d(o.fw_taper_x), d(o.fw_taper_y)
+        s.sa_wx, s.sa_wy = d(o.sa_wx), d(o.sa_wy)
+        s.beta_tvd = o.beta_tvd
+        _lib.check(self.lib.asg_set_step_operators(self.h, slot, C.byref(s)))
+
+    def add_screen(self, z, phase, amp=None):
+        ph = np.ascontiguousarray(phase, dtype=np.float32)
+        am = None if amp is None else np.ascontiguousarray(amp, dtype=np.float32)
+        assert ph.shape == self.shape[:2]
+        _lib.check(self.lib.asg_add_screen(self.h, float(z), _lib.fptr(ph), _lib.fptr(am)))
+        self.n_screens += 1
+
+    def add_source(self, z, plane):
+        pl = np.ascontiguousarray(plane, dtype=np.float32)
+        assert pl.shape == self.shape
+        _lib.check(self.lib.asg_add_source(self.h, float(z), _lib.fptr(pl)))
+
+    def run(self, initial_field, prop_dist, dz, callback=None):
+        u0 = np.ascontiguousarray(initial_field, dtype=np.float32)
+        assert u0.shape == self.shape
+        n = C.c_int(0)
+        cb = _lib.STEP_CB(callback) if callback is not None else _lib.STEP_CB()
+        self._cb = cb
+        _lib.check(self.lib.asg_run(self.h, _lib.fptr(u0), float(prop_dist), float(dz), cb, None,
+                                    C.byref(n)))
+        self.nsteps = n.value
+        return self.nsteps
+
+    def outputs(self, want=("field", "pnp", "ppp", "pI", "pIloss", "zaxis", "pax")):
+        nX, nY, nT = self.shape
+        nz = self.nsteps
+        field = np.empty((nX, nY, nT), np.float32) if "field" in want else None
+        acc = {k: (np.empty((nX, nY, nz), np.float32) if k in want else None)
+               for k in ("pnp", "ppp", "pI", "pIloss")}
+        zaxis = np.empty(nz, np.float64) if "zaxis" in want else None
+        pax = np.empty((nT, nz), np.float32) if "pax" in want else None
+        _lib.check(self.lib.asg_get_outputs(
+            self.h, _lib.fptr(field), _lib.fptr(acc["pnp"]), _lib.fptr(acc["ppp"]),
+            _lib.fptr(acc["pI"]), _lib.fptr(acc["pIloss"]), _lib.dptr(zaxis), _lib.fptr(pax)))
+        return field, acc["pnp"], acc["ppp"], acc["pI"], acc["pIloss"], zaxis, pax
+
+    def last_run_ms(self):
+        v = C.c_double(0)
+        _lib.check(self.lib.asg_last_run_ms(self.h, C.byref(v)))
+        return v.value
+
+    def set_profiling(self, enable: bool):
+        _lib.check(self.lib.asg_set_profiling(self.h, int(enable)))
+
+    def kernel_stats(self):
+        """{kind: (device ms, launches)} of the last run."""
+        n = len(_lib.KERNEL_KINDS)
+        ms = (C.c_double * n)()
+        cnt = (C.c_long * n)()
+        _lib.check(self.lib.asg_kernel_stats(self.h, ms, cnt, n))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(_lib.KERNEL_KINDS)}
+
+    def apply_operator(self, op: int, field, screen_index: int = 0):
+        """One step operator on a field (see asg_apply_operator)."""
+        u = np.array(field, dtype=np.float32, order="C", copy=True)
+        sc = C.c_double(0.0)
+        _lib.check(self.lib.asg_apply_operator(self.h, op, _lib.fptr(u), screen_index,
+                                               C.byref(sc)))
+        return sc.value if op == 8 else u
+
+
+def _torch_view(ptr, shape):
+    import torch
+
+    class _Dev:
+        __cuda_array_interface__ = {
+            "shape": tuple(shape), "typestr": "<f4", "data": (int(ptr), False), "version": 3,
+        }
+    return torch.as_tensor(_Dev(), device="cuda")
+
+
+def angular_spectrum_solve(
+        initial_field: np.ndarray,
+        params: SolverParams,
+        verbose: bool = True,
+        per_step_callback: Optional[Callable] = None,
+        tof_ref_trace: Optional[np.ndarray] = None,
+        tof_t_ref_peak_s: Optional[float] = None,
+        tof_env_ratio: Optional[float] = None,
+        taxis: Optional[np.ndarray] = None):
+    """Propagate a 3-D field with the modified angular spectrum method on the GPU.
+
+    Returns ``(field, pnp, ppp, pI, pIloss, zaxis, pax)`` exactly as the
+    reference does (``:1556-1567``): field (nX,nY,nT) float32, pnp/ppp/pI/pIloss
+    (nX,nY,nZ) float32, zaxis (nZ,) float64, pax (nT,nZ) float32.
+    """
+    if tof_ref_trace is not None and tof_t_ref_peak_s is None:
+        raise ValueError('tof_t_ref_peak_s is required when tof_ref_trace is provided')
+    if tof_ref_trace is not None or tof_env_ratio is not None:
+        raise NotImplementedError(
+            "time-of-flight extraction needs the tof_extraction module, which is not part of "
+            "the reference tree")
+    u0 = np.ascontiguousarray(initial_field, dtype=np.float32)
+    if u0.ndim != 3:
+        raise ValueError("initial_field must be (nX, nY, nT)")
+    nX, nY, nT = u0.shape
+    dz = initial_step(initial_field, params)
+    steps = step_sequence(params.propDist, dz)
+    plan = Plan(u0.shape, params)
+    try:
+        plan.set_operators(0, dz)
+        partial = [s for s in steps if abs(s - dz) > 1e-15]
+        if partial:
+            plan.set_operators(1, partial[-1])
+        if params.phaseScreens is not None:
+            for scr in params.phaseScreens:
+                amp = scr[2] if len(scr) > 2 else None
+                plan.add_screen(scr[0], scr[1], amp)
+        if params.sourcePlanes is not None:
+            for z, plane in params.sourcePlanes:
+                plan.add_source(z, plane)
+        cb = None
+        if per_step_callback is not None:
+            def cb(user, step, z, ptr):
+                per_step_callback(step, z, _torch_view(ptr, (nX, nY, nT)))
+        t0 = _time.time()
+        plan.run(u0, params.propDist, dz, cb)
+        out = plan.outputs()
+        if verbose:
+            z = 0.0
+            for cc, d in enumerate(steps):
+                print(f'z = {z + d:.6f} m  (step {cc})')
+                z += d
+            print(f'Simulation completed in {_time.time() - t0:.2f} s  ({len(steps)} steps)')
+        return out
+    finally:
+        plan.close()

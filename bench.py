@@ -1,0 +1,286 @@
+"""Benchmark of the GB300 angular-spectrum march.
+
+Workload (the plain method at GPU scale, the metric's configuration):
+512 x 512 x 1024 float32 grid, dX = dY = 1.5e-4 m, dT = 1e-8 s, f0 = 2 MHz,
+water-like medium c0 = 1540 m/s, rho0 = 1000, beta = 3.5, alpha0 = 0.5
+dB/cm/MHz (y = 1); a 20 mm piston focused at 60 mm by a quadratic delay,
+5-cycle Gaussian burst, 2 MPa; Strang splitting, KT flux, frequency-weighted
+and super-absorbing boundaries, dZ = 1e-4 m.  Synthetic, seeded input.
+
+One "step" = one march step (three spectral stages over the 268 M-voxel
+field, plus boundaries and accumulators).  The field (1 GiB) and its
+spectrum are larger than L2, so no flush is needed between steps.
+
+Lines printed (one JSON line):
+  default         GPU arm: value = voxel-steps/s measured with CUDA events over
+                  exactly K march steps after W warm-up steps; e2e through the
+                  public API with host buffers; roofline of the dominant kernel;
+                  CPU baseline (the oracle port on a bounded sample).
+  --impl reference  the CPU reference path (the oracle port of the reference's
+                  algorithm, all host threads) on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+NX, NY, NT = 512, 512, 1024
+V = NX * NY * NT
+B_ALG = 48.0  # algorithmic bytes per voxel-step of the Strang path (3 stages x 2 sweeps x 8 B)
+B_SWEEP = 8.0  # algorithmic bytes per voxel of one pass (read 4 + write 4)
+METRIC = "voxel-steps/s"
+
+
+def workload_params():
+    from angularspectrum_heterogeneous_gb300 import SolverParams
+    return SolverParams(dX=1.5e-4, dY=1.5e-4, dT=1e-8, c0=1540.0, rho0=1000.0, beta=3.5,
+                        alpha0=0.5, attenPow=1.0, f0=2e6, propDist=0.07, dZmin=1e-4,
+                        fluxScheme="kt", useFreqWeightedBoundary=True, useSuperAbsorbing=True)
+
+
+def workload_field():
+    import scenarios as S
+    return S.piston_field(NX, NY, NT, 1.5e-4, 1.5e-4, 1e-8, 2e6, 2e6, radius=20e-3,
+                          focus=60e-3, ncycles=5)
+
+
+def config(extra=None):
+    c = {"workload": "plain KT march, 512x512x1024 focused piston 2 MPa, f0 2 MHz, "
+                     "freq-weighted + super-absorbing, dZ 1e-4 m (configs[1])",
+         "grid": [NX, NY, NT], "voxels": V, "l2": "field and spectrum (1 GiB each) exceed L2; "
+                                                    "no flush needed", "parallelism": "1 GPU"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port of the reference on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(nsteps=1, threads=None):
+    """One (or a few) march steps of the full workload grid by the oracle,
+    operator build excluded from the timing.  Returns (voxel-steps/s, cores, sample)."""
+    import oracle.asm_oracle as O
+    threads = threads or os.cpu_count()
+    O.set_fft_backend("scipy", threads)
+    p = workload_params()
+    op = O.OracleParams(**{k: getattr(p, k) for k in O.OracleParams.__dataclass_fields__})
+    op.propDist = nsteps * op.dZmin
+    u0 = workload_field()
+    # time the march only: build the operators first, then run
+    t_build0 = time.time()
+    st = O.OracleSolveState(u0, op, "fp32") if hasattr(O, "OracleSolveState") else None
+    if st is not None:
+        tb = time.time() - t_build0
+        t0 = time.time()
+        st.march(nsteps)
+        dt = time.time() - t0
+    else:
+        t0 = time.time()
+        O.solve(u0, op, "fp32")
+        dt = time.time() - t0
+        tb = 0.0
+    O.set_fft_backend("numpy")
+    return V * nsteps / dt, threads, (f"{nsteps} march step(s) of the {NX}x{NY}x{NT} workload, "
+                                      f"oracle port (numpy + scipy.fft, {threads} threads), "
+                                      f"operator build ({tb:.1f} s) excluded")
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        pass  # the CPU path has no warm-up effects worth a full step
+    for _ in range(args.steps):
+        v, cores, sample = cpu_sample(1)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "voxel-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": V / v * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(),
+            "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args):
+    import torch
+    from angularspectrum_heterogeneous_gb300 import Plan, angular_spectrum_solve
+    from angularspectrum_heterogeneous_gb300.solver import initial_step
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    params = workload_params()
+    u0 = workload_field()
+    dz = initial_step(u0, params)
+    plan = Plan((NX, NY, NT), params)
+    plan.set_operators(0, dz)
+    # warm-up: W march steps
+    plan.run(u0, args.warmup * dz, dz)
+    # timed: exactly K march steps, CUDA events on the library's stream
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks() as clk:
+        plan.run(u0, args.steps * dz, dz)
+    torch.cuda.synchronize()
+    ms = plan.last_run_ms()
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms = float(t.item())
+    launches = sum(v[1] for v in plan.kernel_stats().values())
+    # per-kernel device times (separate profiled pass of the same K steps)
+    plan.set_profiling(True)
+    plan.run(u0, args.steps * dz, dz)
+    stats = plan.kernel_stats()
+    plan.set_profiling(False)
+    plan.close()
+    del plan
+    value = world * V * args.steps / (ms / 1e3)
+
+    # e2e: public API, host buffers in and out, K steps
+    p2 = workload_params()
+    p2.propDist = args.steps * dz
+    torch.cuda.synchronize()
+    t0 = time.time()
+    out = angular_spectrum_solve(u0, p2, verbose=False)
+    torch.cuda.synchronize()
+    e2e_s = time.time() - t0
+    h2d = u0.nbytes / args.steps
+    d2h = sum(a.nbytes for a in out) / args.steps
+
+    peak, peak_kind = peaks()
+    kinds = {k: v for k, v in stats.items() if v[1] > 0 and k != "other"}
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms = kinds[dom][0] / kinds[dom][1]
+    achieved = V * B_SWEEP / (dom_ms / 1e3) / 1e9
+    per_kernel = {k: {"ms_per_launch": v[0] / max(v[1], 1), "launches": v[1],
+                      "GBps_alg": (V * B_SWEEP / (v[0] / max(v[1], 1) / 1e3) / 1e9)
+                      if v[0] > 0 else None}
+                  for k, v in stats.items() if v[1] > 0}
+    line = {"metric": METRIC, "value": value, "unit": "voxel-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config({"step_ms_profiled": sum(
+                v[0] for v in stats.values()) / args.steps}),
+            "hbm_GBps_alg": value * B_ALG / 1e9,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": dom,
+                         "peak_source": peak_kind,
+                         "step_frac": value * B_ALG / 1e9 / peak},
+            "kernels": per_kernel,
+            "e2e": {"value": V * args.steps / e2e_s, "unit": "voxel-steps/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary()}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, sample = cpu_sample(1)
+        line["cpu_baseline"] = {"value": v, "unit": "voxel-steps/s", "cores": cores,
+                                "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * asg_gb300.h -- C ABI of the GB300 angular-spectrum march.
+ *
+ * One plan = one grid (nX, nY, nT) and one option set.  The plan owns all
+ * device memory; the caller owns every host buffer it passes.  A plan is not
+ * thread-safe: use one plan per host thread.  Every entry point returns an
+ * asg_status (0 = OK, negative = error); asg_last_error() gives the message of
+ * the last failure on the calling thread.
+ *
+ * The entry points replace the reference's Python call stack of the march
+ * (angular_spectrum_solver.py of pinton-lab/angularspectrum_heterogeneous):
+ *   asg_plan_create      <- angular_spectrum_solve set-up, :1283-1296, and
+ *                           SolverParams, :35-76
+ *   asg_set_step_operators <- _build_operators / _to_jax, :1301-1371
+ *                           (precalculate_mas :396-462, precalculate_abl :116-138,
+ *                            precalculate_ad(_pow2) :468-592, precalculate_abl_freq
+ *                            :144-179, _make_boundary_weights :275-284,
+ *                            precalculate_obliquity_map :598-627)
+ *   asg_add_screen       <- SolverParams.phaseScreens and :1505-1518
+ *   asg_add_source       <- SolverParams.sourcePlanes and :1521-1527
+ *   asg_run              <- the march loop, :1408-1550
+ *   asg_get_outputs      <- the trimmed return tuple, :1556-1567
+ *   asg_apply_operator   <- one step operator on a field: _angular_spectrum_step
+ *                           :649-655, _attenuation_step :667-685,
+ *                           _freq_weighted_boundary_step :658-664,
+ *                           _super_absorbing_step :185-272, _apply_phase_screen
+ *                           :352-390
+ *   asg_flux_columns     <- _rusanov_flux_standard :688-696, _rusanov_flux_tvd
+ *                           :699-724, _kt_flux :833-839, _kt_flux_minmod
+ *                           :862-868, _kt_flux_adaptive :842-859
+ */
+#ifndef ASG_GB300_H
+#define ASG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ASG_OK = 0,
+  ASG_ERR_ARG = -1,        /* bad argument (null pointer, unknown option) */
+  ASG_ERR_SHAPE = -2,      /* grid shape not supported */
+  ASG_ERR_NAN = -3,        /* non-finite value in the field */
+  ASG_ERR_STABILITY = -4,  /* N dZ/dT max|p| > stabilityThreshold (the reference restarts forever) */
+  ASG_ERR_TIMEOUT = -5,    /* a bounded device wait gave up */
+  ASG_ERR_CUDA = -6,       /* CUDA runtime error */
+  ASG_ERR_STATE = -7,      /* call out of order (e.g. run before operators) */
+  ASG_ERR_NOMEM = -8       /* device allocation failed */
+} asg_status;
+
+typedef struct asg_plan asg_plan;
+
+/* Flux schemes (SolverParams.fluxScheme/useTVD/useSplitStep select among these). */
+enum {
+  ASG_FLUX_RUSANOV = 1,      /* _rusanov_flux_standard */
+  ASG_FLUX_RUSANOV_TVD = 2,  /* _rusanov_flux_tvd */
+  ASG_FLUX_KT = 3,           /* _kt_flux (MUSCL-MC) */
+  ASG_FLUX_KT_MINMOD = 4     /* _kt_flux_minmod */
+};
+
+/* Options of one solve.  Doubles are SI units as in SolverParams. */
+typedef struct {
+  int nX, nY, nT;
+  double dX, dY, dT, c0, rho0, beta, f0;
+  int split_step;            /* useSplitStep */
+  int flux;                  /* ASG_FLUX_* for the nonlinear step */
+  int boundary_layer;        /* useBoundaryLayer */
+  int freq_weighted;         /* useFreqWeightedBoundary */
+  int super_absorbing;       /* useSuperAbsorbing */
+  double super_absorbing_strength;
+  int nonlinear_obliquity;   /* useNonlinearityObliquity */
+  double stability_threshold;
+  double adaptive_filter_strength; /* enters the per-step TVD parameter beta_tvd */
+  double kt_cfl_target;      /* > 0: per-column KT sub-cycling at this CFL (extension) */
+  int kt_max_subcycles;
+  int pax_x, pax_y;          /* column recorded in pax (reference: nX//2, nY//2) */
+} asg_config;
+
+/* 1-D operator description for one step size, all FP64, built on the host
+ * (the device expands them into its multiplier tables). */
+typedef struct {
+  double dz;                 /* step size these operators are for */
+  const double* kx;          /* [nX] centred grid of precalculate_mas, :405-406 */
+  const double* ky;          /* [nY] */
+  const double* kt;          /* [nT] centred temporal grid (/c0), :403-404 */
+  double kfilt_start;        /* cosine k-filter start (k_trans_start) */
+  double kfilt_max;          /* k_trans_max */
+  const double* alpha;       /* [nT] alpha(f_m), f_m = m/(nT dT) */
+  const double* alpha_star;  /* [nT] alphaStar(f_m) */
+  int atten_obliquity;       /* useObliquityCorrection */
+  int atten_clip_negative;   /* water model clips Re<0 to 0 */
+  const double* abl_x;       /* [nX] 1-D taper (all ones without a boundary layer) */
+  const double* abl_y;       /* [nY] */
+  const double* abl_t;       /* [nT] */
+  const double* fw_exponent; /* [nT/2+1] freq-weighted exponent per bin (or NULL) */
+  const double* fw_taper_x;  /* [nX] taper of the freq-weighted mask */
+  const double* fw_taper_y;  /* [nY] */
+  const double* sa_wx;       /* [nX] super-absorbing weights (or NULL) */
+  const double* sa_wy;       /* [nY] */
+  double beta_tvd;           /* unused: the driver forms beta_tvd per step */
+} asg_step_operators;
+
+/* Plan lifecycle */
+int asg_plan_create(const asg_config* cfg, asg_plan** out);
+int asg_plan_destroy(asg_plan* plan);
+
+/* Operators for the regular step (slot 0) and for a partial last step (slot 1). */
+int asg_set_step_operators(asg_plan* plan, int slot, const asg_step_operators* ops);
+
+/* Phase/amplitude screen at depth z: phase[nX*nY], amp[nX*nY] or NULL. */
+int asg_add_screen(asg_plan* plan, double z, const float* phase, const float* amp);
+
+/* Dense source plane at depth z_mid: plane[nX*nY*nT]; stored compressed to
+ * its non-zero columns. */
+int asg_add_source(asg_plan* plan, double z, const float* plane);
+
+/* Per-step callback: step index, z after the step, device pointer to the real
+ * field (nX*nY*nT float32, valid during the call). */
+typedef void (*asg_step_cb)(void* user, int step, double z, const float* dev_field);
+
+/* March from the given initial field (host, nX*nY*nT float32) over propDist
+ * with step dZ (last step partial if needed).  n_steps_out receives the step
+ * count; the outputs stay on the device until asg_get_outputs. */
+int asg_run(asg_plan* plan, const float* initial_field, double prop_dist, double dz,
+            asg_step_cb cb, void* user, int* n_steps_out);
+
+/* Copy the outputs of the last run into host buffers laid out as the
+ * reference returns them: field (nX,nY,nT), pnp/ppp/pI/pIloss (nX,nY,nZ),
+ * zaxis (nZ), pax (nT,nZ).  Any pointer may be NULL to skip it. */
+int asg_get_outputs(asg_plan* plan, float* field, float* pnp, float* ppp, float* pI,
+                    float* pIloss, double* zaxis, float* pax);
+
+/* Device time of the last run's march in milliseconds (CUDA events). */
+int asg_last_run_ms(asg_plan* plan, double* ms);
+
+/* Kernel kinds of one march step, for asg_kernel_stats. */
+enum {
+  ASG_K_XY_A = 0,      /* plane pass opening the step (+ stability test) */
+  ASG_K_T_NONLIN = 1,  /* column pass with the Burgers step */
+  ASG_K_XY_B = 2,      /* second half-step diffraction plane pass (Strang) */
+  ASG_K_T_MID = 3,     /* column pass with the taper only (Strang) */
+  ASG_K_XY_C = 4,      /* attenuation plane pass + boundary/screen epilogue */
+  ASG_K_T_END = 5,     /* column pass closing the step (sources, accumulators) */
+  ASG_K_OTHER = 6,     /* bookkeeping and beam-obliquity passes */
+  ASG_NKINDS = 7
+};
+
+/* Record CUDA events around every kernel launch of subsequent runs. */
+int asg_set_profiling(asg_plan* plan, int enable);
+
+/* Per kind: summed device milliseconds (profiling on) and launch counts of
+ * the last run (counts are kept whether or not profiling is on). */
+int asg_kernel_stats(asg_plan* plan, double* ms, long* launches, int nkinds);
+
+/* One step operator on a host field in place (uses the slot-0 operators):
+ * op = 1 full diffraction (HH, abl), 2 half diffraction (HH_half, abl_half),
+ *      3 full attenuation, 4 half attenuation, 5 frequency-weighted boundary,
+ *      6 super-absorbing boundary, 7 phase screen `screen_index`,
+ *      8 beam-obliquity scalar (result in *scalar_out, field unchanged). */
+int asg_apply_operator(asg_plan* plan, int op, float* field, int screen_index,
+                       double* scalar_out);
+
+/* Burgers step on ncols independent columns of length nT (host in/out). */
+int asg_flux_columns(const float* in, float* out, int ncols, int nT, int flux, double n_coef,
+                     double dz, double dt, double beta_tvd, double cfl_target, int max_subcycles);
+
+/* Message of the last error on this thread. */
+const char* asg_last_error(void);
+
+/* Library build description (arch, kernels compiled in). */
+const char* asg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASG_GB300_H */

@@ -61,7 +61,8 @@ def piston_field(nX, nY, nT, dX, dY, dT, f0, p0, radius, focus, ncycles=3, dur=2
     X, Y = np.meshgrid(x, y, indexing="ij")
     r2 = X ** 2 + Y ** 2
     ap = (r2 <= radius ** 2).astype(np.float64)
-    delay = -(r2 / (2.0 * focus * c0)) + X * np.sin(steer) / c0
+    # converging wave: the rim fires first (pulse centre at t = -delay)
+    delay = (r2 / (2.0 * focus * c0)) + X * np.sin(steer) / c0
     delay = np.where(ap > 0, delay - delay[ap > 0].mean(), 0.0)
     w0 = 2 * np.pi * f0
     tt = t[None, None, :] + delay[:, :, None]
