@@ -3,9 +3,9 @@
 //
 // Multiplier of one mode (kx, ky, bin f), built in FP64 and rounded once:
 //   propagator (precalculate_mas, angular_spectrum_solver.py:396-462)
-//     kk < k^2 : 2 * mask(kk) * exp(i dz kk / (k + sqrt(k^2 - kk)))
+//     kk < k^2 : mask(kk) * exp(i dz kk / (k + sqrt(k^2 - kk)))
 //                (the cancellation-free form of exp(i dz (k - kz)), :441)
-//     else     : 2 * mask(kk) * exp(-dz sqrt(kk - k^2)) * exp(i dz k)   (:440)
+//     else     : mask(kk) * exp(-dz sqrt(kk - k^2)) * exp(i dz k)   (:440)
 //     zero for bins 0 and nT/2 (:455), k = centred temporal grid value of the
 //     bin (:403-404), mask = cosine k-filter sized from the full step (:410-433)
 //   attenuation/KK (_build_oblique_atten_filter, :468-520)
@@ -48,8 +48,10 @@ __global__ void k_build_table(TableParams p) {
         }
         double s, c;
         sincos(ph, &s, &c);
-        re = 2.0 * mask * amp * c;
-        im = 2.0 * mask * amp * s;
+        // the reference's factor 2 on the kept bins is cancelled by the real
+        // part it takes afterwards (Re(ifftn) = ifftn of (W(k)+conj W(-k))/2)
+        re = mask * amp * c;
+        im = mask * amp * s;
       }
     }
     if (p.use_att) {

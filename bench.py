@@ -37,6 +37,13 @@ sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
 NX, NY, NT = 512, 512, 1024
 V = NX * NY * NT
+
+
+def set_grid(nx, ny, nt):
+    """Override the grid (small cases for profiler captures only)."""
+    global NX, NY, NT, V
+    NX, NY, NT = nx, ny, nt
+    V = NX * NY * NT
 B_ALG = 48.0  # algorithmic bytes per voxel-step of the Strang path (3 stages x 2 sweeps x 8 B)
 B_SWEEP = 8.0  # algorithmic bytes per voxel of one pass (read 4 + write 4)
 METRIC = "voxel-steps/s"
@@ -224,15 +231,17 @@ def run_gpu_arm(args):
     value = world * V * args.steps / (ms / 1e3)
 
     # e2e: public API, host buffers in and out, K steps
-    p2 = workload_params()
-    p2.propDist = args.steps * dz
-    torch.cuda.synchronize()
-    t0 = time.time()
-    out = angular_spectrum_solve(u0, p2, verbose=False)
-    torch.cuda.synchronize()
-    e2e_s = time.time() - t0
-    h2d = u0.nbytes / args.steps
-    d2h = sum(a.nbytes for a in out) / args.steps
+    e2e_s, h2d, d2h = float("nan"), 0, 0
+    if not args.no_e2e:
+        p2 = workload_params()
+        p2.propDist = args.steps * dz
+        torch.cuda.synchronize()
+        t0 = time.time()
+        out = angular_spectrum_solve(u0, p2, verbose=False)
+        torch.cuda.synchronize()
+        e2e_s = time.time() - t0
+        h2d = u0.nbytes / args.steps
+        d2h = sum(a.nbytes for a in out) / args.steps
 
     peak, peak_kind = peaks()
     kinds = {k: v for k, v in stats.items() if v[1] > 0 and k != "other"}
@@ -275,7 +284,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--grid", type=int, nargs=3, default=None,
+                    help="profiling only: a smaller grid with the same options")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    if args.grid:
+        set_grid(*args.grid)
     if args.impl == "reference":
         run_reference_arm(args)
     else:
