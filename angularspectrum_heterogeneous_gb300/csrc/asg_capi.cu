@@ -176,7 +176,9 @@ struct asg_plan {
   asg_config cfg;
   int X, Y, T, ncols, F, M;
   bool tfast, xyfast;
-  int G;
+  bool split;  // half-plane transforms: the column pass applies the first radix-2 x stage
+  int G, nsub;
+  float2* spec2 = nullptr;  // whole-plane output of the epilogue pass
   GenPlan gp_t, gp_x, gp_y;
   cudaStream_t st;
   cudaEvent_t ev0, ev1;
@@ -293,7 +295,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.map);
     cudaFree(s.val);
   }
-  void* ptrs[] = {p->spec, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+  void* ptrs[] = {p->spec, p->spec2, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
@@ -333,8 +335,15 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   p->F = T / 2 + 1;
   p->M = T / 2;
   p->N = cfg->beta / (2.0 * cfg->c0 * cfg->c0 * cfg->c0 * cfg->rho0);
-  p->tfast = asg_t_fast_supported(T);
-  p->xyfast = asg_xy_fast_supported(X, Y, &p->G);
+  p->tfast = asg_t_fast_supported(T) && X % 2 == 0 && Y % 4 == 0;
+  int Gs = 0;
+  p->split = p->tfast && asg_xy_split_supported(X, Y, &Gs);
+  p->xyfast = p->split || asg_xy_fast_supported(X, Y, &p->G);
+  p->nsub = 1;
+  if (p->split) {
+    p->G = Gs;
+    p->nsub = 2;
+  }
   if (!p->xyfast) {
     p->G = 1;
     if (asg_xy_generic_smem(X, Y) > 200 * 1024)
@@ -368,28 +377,40 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
     for (int q = 0; q < p->F; ++q) p->h_f_of_plane[q] = q;
   }
   // ---- x/y slot -> natural bin, and mirror classes ----
-  auto slot_bins = [](int n, bool fast_xy_x, bool fast_y, int G, std::vector<int>& bin) {
-    bin.resize(n);
-    for (int s = 0; s < n; ++s) {
-      if (fast_xy_x) {
-        const int R = n / G;
-        bin[s] = (s / R) + G * (s % R);
-      } else if (fast_y) {
-        int n1, n2;
-        fast_factors(n, &n1, &n2);
-        bin[s] = (s / n2) + n1 * (s % n2);
-      } else {
-        bin[s] = s;
-      }
+  // natural bin held by each x slot (row order of the plane kernels) and by
+  // each y slot (the fast kernels keep y in four-step slot order)
+  std::vector<int> binx(X), biny(Y);
+  for (int s = 0; s < X; ++s) {
+    if (p->split) {
+      const int Xs = X / 2, R = 16, h = s / Xs, sg = s % Xs;
+      binx[s] = 2 * ((sg / R) + p->G * (sg % R)) + h;
+    } else if (p->xyfast) {
+      const int R = 32;
+      binx[s] = (s / R) + p->G * (s % R);
+    } else {
+      binx[s] = s;
     }
-  };
-  std::vector<int> binx, biny;
-  slot_bins(X, p->xyfast, false, p->G, binx);
-  slot_bins(Y, false, p->xyfast, 1, biny);
-  // mirror classes: slots whose bins sit at centred-grid positions i and
-  // n-1-i share k^2 (the reference's centred grid is symmetric); class id =
-  // the smaller slot of the pair, so consecutive slots read consecutive
-  // table entries
+  }
+  for (int s = 0; s < Y; ++s) {
+    if (p->xyfast) {
+      int n1, n2;
+      fast_factors(Y, &n1, &n2);
+      biny[s] = (s / n2) + n1 * (s % n2);
+    } else {
+      biny[s] = s;
+    }
+  }
+  // x classes: centred-grid index pair {i, X-1-i} (equal kx^2), id = min
+  p->ncx = (X + 1) / 2;
+  p->h_cls_x.resize(X);
+  p->h_rep_x.resize(p->ncx);
+  for (int c = 0; c < p->ncx; ++c) p->h_rep_x[c] = c;
+  for (int s = 0; s < X; ++s) {
+    const int i = (binx[s] + X / 2) % X;
+    p->h_cls_x[s] = i < X - 1 - i ? i : X - 1 - i;
+  }
+  // y classes: the smaller slot of each mirror pair, so consecutive slots read
+  // consecutive table entries
   auto classes = [](int n, const std::vector<int>& bin, std::vector<int>& cls, int& ncls,
                     std::vector<int>& rep) {
     std::vector<int> slot_of_cent(n), cent(n);
@@ -412,12 +433,12 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
     cls.resize(n);
     for (int s = 0; s < n; ++s) cls[s] = id[raw[s]];
   };
-  classes(X, binx, p->h_cls_x, p->ncx, p->h_rep_x);
   classes(Y, biny, p->h_cls_y, p->ncy, p->h_rep_y);
 
   // ---- device buffers ----
   const size_t nspec = (size_t)p->F * p->ncols;
   CKS(dalloc(&p->spec, nspec));
+  if (p->split) CKS(dalloc(&p->spec2, nspec));
   CKS(dalloc(&p->real, (size_t)p->ncols * T));
   std::vector<float2> w;
   roots(T, w);
@@ -527,7 +548,8 @@ static int build_table(asg_plan* p, Slot& s, float2* out, bool prop, double dz_p
   tp.use_att = att;
   tp.obliquity = s.att_obl;
   tp.clip_negative = s.att_clip;
-  tp.norm = 1.0 / ((double)p->X * (double)p->Y);
+  // the plane kernels transform X/nsub-row (sub-)planes
+  tp.norm = 1.0 / ((double)(p->X / p->nsub) * (double)p->Y);
   tp.out = out;
   return asg_launch_table(tp, p->st);
 }
@@ -699,8 +721,14 @@ static TParams tparams(asg_plan* p) {
   TParams t;
   memset(&t, 0, sizeof(t));
   t.spec = p->spec;
+  t.spec_out = nullptr;
   t.ncols = p->ncols;
   t.nT = p->T;
+  t.X = p->X;
+  t.Y = p->Y;
+  t.twX = p->twX;
+  t.split_in = p->split;
+  t.split_out = p->split;
   t.tw = p->twT;
   t.twM = p->twM;
   t.status = p->d_status;
@@ -728,6 +756,7 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.X = p->X;
   x.Y = p->Y;
   x.G = p->G;
+  x.nsub = p->nsub;
   x.nplanes = p->F;
   x.nT = p->T;
   x.f_of_plane = p->f_of_plane;
@@ -843,11 +872,42 @@ static int status_to_error(asg_plan* p) {
 }
 
 // one march step; `last` -> write the real field, no forward transform
+// closing plane pass + (x, y, omega) epilogue, then the column pass that
+// ends the step (or, for asg_apply_operator, just returns to real space)
+static int closing_stage(asg_plan* p, const float2* table, int epi, int nscr, int kind,
+                         TParams& t_after) {
+  XYParams x = xyparams(p, table, false);
+  if (!p->split) {
+    x.epi = epi;
+    x.nscreens = nscr;
+    x.screens = p->d_screens;
+    CKS(run_xy(p, x, kind));
+    t_after.split_in = 0;
+    return ASG_OK;
+  }
+  CKS(run_xy(p, x, kind));
+  if (epi != 0 || nscr > 0) {
+    // half-planes -> whole planes with the epilogue applied, into spec2
+    XYParams e = xyparams(p, nullptr, false);
+    e.epi = epi;
+    e.nscreens = nscr;
+    e.screens = p->d_screens;
+    KScope k(p, ASG_K_OTHER);
+    CKS(asg_launch_epilogue_pass(e, p->spec, p->spec2, 1, p->st));
+    t_after.spec = p->spec2;
+    t_after.spec_out = p->spec;
+    t_after.split_in = 0;
+  } else {
+    t_after.split_in = 1;
+  }
+  return ASG_OK;
+}
+
 static int march_step(asg_plan* p, const Slot& s, double dzs, double btvd, int nscr, int nsrc,
                       bool last, bool want_real) {
-  const bool split = p->cfg.split_step != 0;
-  const float* axy = split ? p->abl_xy_half : p->abl_xy_full;
-  const float* at = split ? p->abl_t_half : p->abl_t_full;
+  const bool strang = p->cfg.split_step != 0;
+  const float* axy = strang ? p->abl_xy_half : p->abl_xy_full;
+  const float* at = strang ? p->abl_t_half : p->abl_t_full;
   // stage A (+ stability test)
   {
     XYParams x = xyparams(p, s.tabA, true);
@@ -857,7 +917,7 @@ static int march_step(asg_plan* p, const Slot& s, double dzs, double btvd, int n
     CKS(run_xy(p, x, ASG_K_XY_A));
   }
   CKS(nonlinear_stage(p, dzs, btvd, axy, at));
-  if (split) {
+  if (strang) {
     XYParams x = xyparams(p, s.tabB, true);
     CKS(run_xy(p, x, ASG_K_XY_B));
     TParams t = tparams(p);
@@ -866,24 +926,17 @@ static int march_step(asg_plan* p, const Slot& s, double dzs, double btvd, int n
     t.do_r2c = 1;
     CKS(run_t(p, t, ASG_K_T_MID));
   }
-  // closing stage: attenuation + (x, y, omega) epilogue
-  {
-    XYParams x = xyparams(p, s.tabC, false);
-    x.epi = (p->cfg.freq_weighted ? EPI_FREQW : 0) | (p->cfg.super_absorbing ? EPI_SUPERABS : 0);
-    x.nscreens = nscr;
-    x.screens = p->d_screens;
-    CKS(run_xy(p, x, ASG_K_XY_C));
-  }
-  {
-    TParams t = tparams(p);
-    t.stats = 1;
-    t.op.nsrc = nsrc;
-    t.op.src = p->d_src;
-    t.write_real = (last || want_real) ? 1 : 0;
-    t.real_out = p->real;
-    t.do_r2c = last ? 0 : 1;
-    CKS(run_t(p, t, ASG_K_T_END));
-  }
+  // closing stage: attenuation + (x, y, omega) epilogue, then the step end
+  const int epi = (p->cfg.freq_weighted ? EPI_FREQW : 0) | (p->cfg.super_absorbing ? EPI_SUPERABS : 0);
+  TParams t = tparams(p);
+  CKS(closing_stage(p, s.tabC, epi, nscr, ASG_K_XY_C, t));
+  t.stats = 1;
+  t.op.nsrc = nsrc;
+  t.op.src = p->d_src;
+  t.write_real = (last || want_real) ? 1 : 0;
+  t.real_out = p->real;
+  t.do_r2c = last ? 0 : 1;
+  CKS(run_t(p, t, ASG_K_T_END));
   KScope k(p, ASG_K_OTHER);
   return asg_launch_advance(p->d_step, p->d_max_cur, p->d_max_next, p->st);
 }
@@ -1065,36 +1118,36 @@ extern "C" int asg_apply_operator(asg_plan* p, int op, float* field, int screen_
   }
   const float* axy = nullptr;
   const float* at = nullptr;
-  XYParams x = xyparams(p, nullptr, false);
+  const float2* table = nullptr;
+  int zero = 0, epi = 0, nscr = 0;
   switch (op) {
     case 1:
     case 2:
       CKS(build_table(p, s, p->tab_scratch, true, op == 1 ? s.dz : s.dz / 2, false, 0.0));
-      x.table = p->tab_scratch;
-      x.zero_dc_nyq = 1;
+      table = p->tab_scratch;
+      zero = 1;
       axy = op == 1 ? p->abl_xy_full : p->abl_xy_half;
       at = op == 1 ? p->abl_t_full : p->abl_t_half;
       break;
     case 3:
     case 4:
       CKS(build_table(p, s, p->tab_scratch, false, 0.0, true, op == 3 ? s.dz : s.dz * 0.5));
-      x.table = p->tab_scratch;
-      x.epi = 0;
+      table = p->tab_scratch;
       break;
-    case 5: x.epi = EPI_FREQW; break;
-    case 6: x.epi = EPI_SUPERABS; break;
+    case 5: epi = EPI_FREQW; break;
+    case 6: epi = EPI_SUPERABS; break;
     case 7: {
       if (screen_index < 0 || screen_index >= (int)p->screens.size())
         return fail(ASG_ERR_ARG, "screen index %d out of range", screen_index);
       ScreenDev sd{p->screens[screen_index].phase, p->screens[screen_index].amp};
       CKS(h2d(p->d_screens, &sd, 1, p->st));
-      x.nscreens = 1;
-      x.screens = p->d_screens;
+      nscr = 1;
       break;
     }
     case 8: {
       if (!p->obl_tab) return fail(ASG_ERR_STATE, "plan built without nonlinear obliquity");
       CK(cudaMemsetAsync(p->power_acc, 0, 2 * sizeof(double), p->st));
+      XYParams x = xyparams(p, nullptr, false);
       x.power_only = 1;
       CKS(run_xy(p, x));
       double acc[2];
@@ -1105,16 +1158,19 @@ extern "C" int asg_apply_operator(asg_plan* p, int op, float* field, int screen_
     }
     default: return fail(ASG_ERR_ARG, "unknown operator %d", op);
   }
-  CKS(run_xy(p, x));
-  {
-    TParams t = tparams(p);
-    t.op.abl_xy = axy;
-    t.op.abl_t = at;
-    t.write_real = 1;
-    t.real_out = p->real;
-    t.do_r2c = 0;
-    CKS(run_t(p, t));
+  TParams t = tparams(p);
+  if (zero) {
+    XYParams x = xyparams(p, table, true);
+    CKS(run_xy(p, x));
+  } else {
+    CKS(closing_stage(p, table, epi, nscr, ASG_K_OTHER, t));
   }
+  t.op.abl_xy = axy;
+  t.op.abl_t = at;
+  t.write_real = 1;
+  t.real_out = p->real;
+  t.do_r2c = 0;
+  CKS(run_t(p, t));
   CK(cudaMemcpyAsync(field, p->real, n * sizeof(float), cudaMemcpyDeviceToHost, p->st));
   CK(cudaStreamSynchronize(p->st));
   return status_to_error(p);

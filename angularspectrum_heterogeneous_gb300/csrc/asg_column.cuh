@@ -64,7 +64,7 @@ struct ColumnOps {
 template <int N2>
 struct PaddedColumn {
   float* base;
-  ASG_DEV int idx(int t) const { int j = t >> 1; return 2 * (j + j / N2) + (t & 1); }
+  ASG_DEV int idx(int t) const { int j = t >> 1; return 2 * (j + 2 * (j / N2)) + (t & 1); }
   ASG_DEV float get(int t) const { return base[idx(t)]; }
   ASG_DEV void set(int t, float v) const { base[idx(t)] = v; }
 };
@@ -120,126 +120,99 @@ ASG_DEV float kt_fh(float um, float up) {
 }
 
 // ---------------------------------------------------------------------------
-// Burgers step on one column by one warp.  Each lane owns a contiguous chunk
-// [t0, t1) of the column; the stencil halo is read from shared memory.  The
-// column end points t=0 and t=nT-1 are never updated (zero boundary rhs).
+// Burgers step on one column by one warp, 32 samples t = t0 + lane at a time.
+// Stencil neighbours come from warp shuffles; across the 32-sample blocks the
+// original values / interface fluxes are carried in registers, so the update
+// runs in place in shared memory with a handful of registers.  The column
+// end points t=0 and t=nT-1 are never updated (zero boundary rhs).
 // ---------------------------------------------------------------------------
-template <int CH, class Col>
+template <class Col>
 ASG_DEV void rusanov_column(const Col& col, int nT, float coef, bool tvd, float beta_tvd,
                             unsigned mask) {
   const int lane = threadIdx.x & 31;
-  const int t0 = lane * CH;
-  float out[CH];
-  // original values in a window [t0-1, t0+CH]
-  float w[CH + 2];
-#pragma unroll
-  for (int i = 0; i < CH + 2; ++i) {
-    int t = t0 - 1 + i;
-    w[i] = (t >= 0 && t < nT) ? col.get(t) : 0.f;
-  }
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = t0 + i;
-    float u = w[i + 1];
-    out[i] = u;
+  float carry = 0.f;  // original u[t0-1]
+  for (int t0 = 0; t0 < nT; t0 += 32) {
+    const int t = t0 + lane;
+    const float u = (t < nT) ? col.get(t) : 0.f;
+    float um = __shfl_up_sync(mask, u, 1);
+    float up = __shfl_down_sync(mask, u, 1);
+    if (lane == 0) um = carry;
+    if (lane == 31) up = (t + 1 < nT) ? col.get(t + 1) : 0.f;
+    float out = u;
     if (t >= 1 && t < nT - 1) {
-      float um = w[i], up = w[i + 2];
       if (!tvd) {
-        float fd = rus_std_fh(u, up) - rus_std_fh(um, u);
-        out[i] = u + (-coef * fd);
+        const float fd = rus_std_fh(u, up) - rus_std_fh(um, u);
+        out = u + (-coef * fd);
       } else {
-        float fd = rus_tvd_fh(u, up) - rus_tvd_fh(um, u);
-        float dm = u - um, dp = up - u;
+        const float fd = rus_tvd_fh(u, up) - rus_tvd_fh(um, u);
+        const float dm = u - um, dp = up - u;
         const float eps = 1e-30f;
-        float r = dp / (dm + eps * sgnf(dm + eps));
-        float ri = dm / (dp + eps * sgnf(dp + eps));
-        float lim = 0.5f * (tvd_phi(r, beta_tvd) + tvd_phi(ri, beta_tvd)) * fd;
-        out[i] = u + (-coef * lim);
+        const float r = dp / (dm + eps * sgnf(dm + eps));
+        const float ri = dm / (dp + eps * sgnf(dp + eps));
+        out = u + (-coef * (0.5f * (tvd_phi(r, beta_tvd) + tvd_phi(ri, beta_tvd)) * fd));
       }
     }
-  }
-  __syncwarp(mask);
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = t0 + i;
-    if (t < nT) col.set(t, out[i]);
+    carry = __shfl_sync(mask, u, 31);
+    __syncwarp(mask);
+    if (t < nT) col.set(t, out);
   }
   __syncwarp(mask);
 }
 
-// rhs of the KT scheme at the lane's CH points from a window of CH+4 values
-template <int CH, bool MC>
-ASG_DEV void kt_rhs_window(const float (&w)[CH + 4], int t0, int nT, float ndt, float (&rhs)[CH]) {
-  // slopes at window positions 1..CH+2  (t0-1 .. t0+CH); zero at the column ends
-  float s[CH + 2];
-#pragma unroll
-  for (int i = 0; i < CH + 2; ++i) {
-    int t = t0 - 1 + i;
-    s[i] = (t >= 1 && t < nT - 1) ? kt_slope<MC>(w[i], w[i + 1], w[i + 2]) : 0.f;
-  }
-  // interface fluxes at t+1/2 for t = t0-1 .. t0+CH-1
-  float fh[CH + 1];
-#pragma unroll
-  for (int i = 0; i < CH + 1; ++i) {
-    float um = w[i + 1] + 0.5f * s[i];
-    float up = w[i + 2] - 0.5f * s[i + 1];
-    fh[i] = kt_fh(um, up);
-  }
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = t0 + i;
-    rhs[i] = (t >= 1 && t < nT - 1) ? (-ndt * (fh[i + 1] - fh[i])) : 0.f;
-  }
-}
-
-template <int CH, bool MC, class Col>
-ASG_DEV void load_window4(const Col& col, int t0, int nT, float (&w)[CH + 4]) {
-#pragma unroll
-  for (int i = 0; i < CH + 4; ++i) {
-    int t = t0 - 2 + i;
-    w[i] = (t >= 0 && t < nT) ? col.get(t) : 0.f;
-  }
-}
-
-// one SSP-RK2 KT step of size dz on the column
-template <int CH, bool MC, class Col>
-ASG_DEV void kt_column_step(const Col& col, int nT, float ndt, float dz, unsigned mask) {
+// rhs of the KT scheme (MUSCL slopes, KT interface fluxes) at t = t0+lane,
+// reading src; fh_carry holds the flux at t0-1/2 from the previous block.
+template <bool MC, class Col>
+ASG_DEV float kt_rhs_lane(const Col& src, int t, int nT, float ndt, float& fh_carry,
+                          float& u_out, unsigned mask) {
   const int lane = threadIdx.x & 31;
-  const int t0 = lane * CH;
-  float w[CH + 4];
-  load_window4<CH, MC>(col, t0, nT, w);
-  float u[CH], rhs[CH];
-#pragma unroll
-  for (int i = 0; i < CH; ++i) u[i] = w[i + 2];
-  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
-  __syncwarp(mask);
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = t0 + i;
-    if (t < nT) col.set(t, u[i] + dz * rhs[i]);  // stage1
+  const float u0 = (t < nT) ? src.get(t) : 0.f;
+  float um1 = __shfl_up_sync(mask, u0, 1);
+  float up1 = __shfl_down_sync(mask, u0, 1);
+  if (lane == 0) um1 = (t >= 1) ? src.get(t - 1) : 0.f;
+  if (lane == 31) up1 = (t + 1 < nT) ? src.get(t + 1) : 0.f;
+  const float sg = (t >= 1 && t < nT - 1) ? kt_slope<MC>(um1, u0, up1) : 0.f;
+  float sn = __shfl_down_sync(mask, sg, 1);
+  if (lane == 31) {
+    const float up2 = (t + 2 < nT) ? src.get(t + 2) : 0.f;
+    sn = (t + 1 >= 1 && t + 1 < nT - 1) ? kt_slope<MC>(u0, up1, up2) : 0.f;
+  }
+  // interface t+1/2
+  const float fh = kt_fh(u0 + 0.5f * sg, up1 - 0.5f * sn);
+  float fp = __shfl_up_sync(mask, fh, 1);
+  if (lane == 0) fp = fh_carry;
+  fh_carry = __shfl_sync(mask, fh, 31);
+  u_out = u0;
+  return (t >= 1 && t < nT - 1) ? (-ndt * (fh - fp)) : 0.f;
+}
+
+// one SSP-RK2 KT step of size dz; stage-1 values go to `stg`
+template <bool MC, class Col>
+ASG_DEV void kt_column_step(const Col& col, const Col& stg, int nT, float ndt, float dz,
+                            unsigned mask) {
+  const int lane = threadIdx.x & 31;
+  float carry = 0.f;
+  for (int t0 = 0; t0 < nT; t0 += 32) {
+    const int t = t0 + lane;
+    float u;
+    const float r = kt_rhs_lane<MC>(col, t, nT, ndt, carry, u, mask);
+    if (t < nT) stg.set(t, u + dz * r);
   }
   __syncwarp(mask);
-  load_window4<CH, MC>(col, t0, nT, w);
-  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
-  __syncwarp(mask);
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = t0 + i;
-    float s1 = w[i + 2];
-    if (t < nT) col.set(t, 0.5f * u[i] + 0.5f * (s1 + dz * rhs[i]));
+  carry = 0.f;
+  for (int t0 = 0; t0 < nT; t0 += 32) {
+    const int t = t0 + lane;
+    float s1;
+    const float r = kt_rhs_lane<MC>(stg, t, nT, ndt, carry, s1, mask);
+    if (t < nT) col.set(t, 0.5f * col.get(t) + 0.5f * (s1 + dz * r));
   }
   __syncwarp(mask);
 }
 
-template <int CH, class Col>
+template <class Col>
 ASG_DEV float column_absmax(const Col& col, int nT) {
   const int lane = threadIdx.x & 31;
   float m = 0.f;
-#pragma unroll
-  for (int i = 0; i < CH; ++i) {
-    int t = lane * CH + i;
-    if (t < nT) m = fmaxf(m, fabsf(col.get(t)));
-  }
+  for (int t = lane; t < nT; t += 32) m = fmaxf(m, fabsf(col.get(t)));
   return warp_max(m);
 }
 
@@ -247,7 +220,8 @@ ASG_DEV float column_absmax(const Col& col, int nT) {
 // The whole column phase.  CH = ceil(nT/32) samples per lane.
 // ---------------------------------------------------------------------------
 template <int CH, class Col>
-ASG_DEV float column_phase(const Col& col, int c, int nT, const ColumnOps& op, bool write_stats) {
+ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const ColumnOps& op,
+                           bool write_stats) {
   const int lane = threadIdx.x & 31;
   const unsigned mask = 0xffffffffu;
   // 1) taper
@@ -270,11 +244,11 @@ ASG_DEV float column_phase(const Col& col, int c, int nT, const ColumnOps& op, b
       ndt = (float)(op.n_kt64 * sc);
     }
     if (op.flux == FLUX_RUSANOV || op.flux == FLUX_RUSANOV_TVD) {
-      rusanov_column<CH>(col, nT, coef_rus, op.flux == FLUX_RUSANOV_TVD, op.beta_tvd, mask);
+      rusanov_column(col, nT, coef_rus, op.flux == FLUX_RUSANOV_TVD, op.beta_tvd, mask);
     } else {
       int nsub = 1;
       if (op.cfl_target > 0.f) {
-        float um = column_absmax<CH>(col, nT);
+        float um = column_absmax(col, nT);
         float cfl = ndt * um * op.dz;
         if (!(cfl <= op.cfl_target || um < 1e-30f)) {
           float q = ceilf(cfl / op.cfl_target);
@@ -285,8 +259,8 @@ ASG_DEV float column_phase(const Col& col, int c, int nT, const ColumnOps& op, b
       }
       float dzs = op.dz / (float)nsub;
       for (int k = 0; k < nsub; ++k) {
-        if (op.flux == FLUX_KT_MC) kt_column_step<CH, true>(col, nT, ndt, dzs, mask);
-        else kt_column_step<CH, false>(col, nT, ndt, dzs, mask);
+        if (op.flux == FLUX_KT_MC) kt_column_step<true>(col, stg, nT, ndt, dzs, mask);
+        else kt_column_step<false>(col, stg, nT, ndt, dzs, mask);
       }
     }
   }

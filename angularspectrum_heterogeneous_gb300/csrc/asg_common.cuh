@@ -122,8 +122,10 @@ ASG_DEV void dft(float2 (&v)[N]) {
   } else {
     constexpr int P = DftSplit<N>::P;
     constexpr int Q = DftSplit<N>::Q;
-    // input n = Q*p + q ; output k = ka + P*kb
-    float2 y[Q][P];
+    // input n = Q*p + q ; output k = ka + P*kb.  Stage 1 runs in place on v
+    // (stride-Q subsequences), stage 2 writes each block straight into its
+    // output positions; with compile-time indices the final permutation is a
+    // register renaming, so about N complex values are live at any time.
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       float2 t[P];
@@ -131,17 +133,20 @@ ASG_DEV void dft(float2 (&v)[N]) {
       for (int p = 0; p < P; ++p) t[p] = v[Q * p + q];
       dft<P, INV>(t);
 #pragma unroll
-      for (int ka = 0; ka < P; ++ka) y[q][ka] = twiddle_mul<N, INV>(t[ka], q * ka);
+      for (int ka = 0; ka < P; ++ka) v[Q * ka + q] = twiddle_mul<N, INV>(t[ka], q * ka);
     }
+    float2 o[N];
 #pragma unroll
     for (int ka = 0; ka < P; ++ka) {
       float2 t[Q];
 #pragma unroll
-      for (int q = 0; q < Q; ++q) t[q] = y[q][ka];
+      for (int q = 0; q < Q; ++q) t[q] = v[Q * ka + q];
       dft<Q, INV>(t);
 #pragma unroll
-      for (int kb = 0; kb < Q; ++kb) v[ka + P * kb] = t[kb];
+      for (int kb = 0; kb < Q; ++kb) o[ka + P * kb] = t[kb];
     }
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = o[i];
   }
 }
 
@@ -152,16 +157,18 @@ ASG_DEV void dft(float2 (&v)[N]) {
 //   forward, step B: for each ka in [0,N1): DFT_N2 over b of slots b + N2 ka,
 //                    stored at slot kb + N2 ka  -> frequency ka + N1 kb
 // The inverse runs B^-1 then A^-1 and takes the permuted slots back to
-// natural order.  Slots are padded by one complex every N2 slots
-// (position s + s/N2) so both access patterns are free of bank conflicts.
+// natural order.  Slots are padded by two complex every N2 slots
+// (position s + 2*(s/N2)): step A's strided 8-byte accesses and step B's
+// contiguous 16-byte accesses are both free of bank conflicts, and an even
+// slot stays 16-byte aligned.
 // ---------------------------------------------------------------------------
 template <int N1_, int N2_>
 struct LinePlan {
   static constexpr int N1 = N1_;
   static constexpr int N2 = N2_;
   static constexpr int N = N1 * N2;
-  static constexpr int PADDED = N + N1;  // padded slots per line
-  ASG_DEV static int pos(int s) { return s + s / N2; }
+  static constexpr int PADDED = N + 2 * N1;  // padded slots per line
+  ASG_DEV static int pos(int s) { return s + 2 * (s / N2); }
   // slot holding frequency k
   __host__ __device__ static int slot_of_freq(int k) { return (k / N1) + N2 * (k % N1); }
   __host__ __device__ static int freq_of_slot(int s) { return (s / N2) + N1 * (s % N2); }
@@ -189,20 +196,26 @@ ASG_DEV void stepA_fwd_smem(float2* line, int b, const float2* tw) {
   dft<PL::N1, false>(v);
 #pragma unroll
   for (int ka = 0; ka < PL::N1; ++ka) {
-    float2 w = tw[(b * ka) % PL::N];
-    line[PL::pos(b + PL::N2 * ka)] = ka == 0 ? v[0] : cmul(v[ka], w);
+    // b*ka <= (N2-1)(N1-1) < N: no reduction needed
+    line[PL::pos(b + PL::N2 * ka)] = ka == 0 ? v[0] : cmul(v[ka], tw[b * ka]);
   }
 }
 
 template <class PL, bool INV>
 ASG_DEV void stepB_smem(float2* line, int ka) {
+  static_assert(PL::N2 % 2 == 0, "step B reads complex pairs");
   float2 v[PL::N2];
-  float2* p = line + ka * (PL::N2 + 1);  // pos(N2*ka) = N2*ka + ka
+  float4* p = reinterpret_cast<float4*>(line + ka * (PL::N2 + 2));  // pos(N2*ka)
 #pragma unroll
-  for (int b = 0; b < PL::N2; ++b) v[b] = p[b];
+  for (int b = 0; b < PL::N2 / 2; ++b) {
+    const float4 q = p[b];
+    v[2 * b] = make_float2(q.x, q.y);
+    v[2 * b + 1] = make_float2(q.z, q.w);
+  }
   dft<PL::N2, INV>(v);
 #pragma unroll
-  for (int b = 0; b < PL::N2; ++b) p[b] = v[b];
+  for (int b = 0; b < PL::N2 / 2; ++b)
+    p[b] = make_float4(v[2 * b].x, v[2 * b].y, v[2 * b + 1].x, v[2 * b + 1].y);
 }
 
 // inverse step A: twiddle conj(W^(b ka)) then inverse DFT_N1 over ka -> a
@@ -212,7 +225,7 @@ ASG_DEV void stepA_inv_smem(float2* line, int b, const float2* tw) {
 #pragma unroll
   for (int ka = 0; ka < PL::N1; ++ka) {
     float2 x = line[PL::pos(b + PL::N2 * ka)];
-    v[ka] = ka == 0 ? x : cmulc(x, tw[(b * ka) % PL::N]);
+    v[ka] = ka == 0 ? x : cmulc(x, tw[b * ka]);
   }
   dft<PL::N1, true>(v);
 #pragma unroll

@@ -14,8 +14,12 @@ struct GenPlan;
 #include "asg_column.cuh"
 
 struct TParams {
-  float2* spec;          // [planes][ncols]
+  float2* spec;          // [planes][ncols] input spectrum (output too unless spec_out)
+  float2* spec_out;      // output spectrum, or null for in place
   int ncols, nT;
+  int X, Y;              // grid (fast kernels tile pairs of columns x, x+X/2)
+  int split_in, split_out;  // first radix-2 x stage undone on input / applied on output
+  const float2* twX;     // W_X^k, k < X
   int in_real;           // read real columns from real_in instead of the spectrum
   const float* real_in;  // [ncols][nT]
   int write_real;        // write the real column to real_out after the column phase
@@ -45,7 +49,9 @@ enum EpiFlags : int {
 
 struct XYParams {
   float2* spec;          // [planes][X][Y]
-  int X, Y, G;           // G CTAs per plane (thread-block cluster), R = X / G rows each
+  int X, Y, G;           // G CTAs per (sub-)plane (thread-block cluster)
+  int nsub;              // sub-planes per plane along x (1, or 2 when the column pass
+                         // applies the first radix-2 stage of the x transform)
   int nplanes;
   int nT;
   const int* f_of_plane; // rfft bin held by each plane
@@ -84,6 +90,10 @@ struct XYParams {
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);
+// half-plane kernels (rows x < X/2 and x >= X/2 transformed separately)
+bool asg_xy_split_supported(int X, int Y, int* G_out);
+int asg_launch_epilogue_pass(const XYParams& p, const float2* src, float2* dst, int split,
+                             cudaStream_t st);
 size_t asg_xy_generic_smem(int X, int Y);
 int asg_launch_xy(const XYParams& p, bool fast, const GenPlan& plx, const GenPlan& ply,
                   cudaStream_t st);

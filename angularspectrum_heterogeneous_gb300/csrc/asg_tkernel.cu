@@ -19,89 +19,122 @@
 ASG_DEFINE_ROOT_UPLOADER(asg_roots_upload_t)
 
 // ---------------------------------------------------------------------------
-// fast kernel: nT = 2M, M = N1*N2 (register-resident four-step FFT)
-// C columns per block, one warp per column
+// fast kernel: nT = 2M, M = N1*N2 (register-resident four-step FFT).
+// A block handles 8 columns: 4 consecutive y at x and the same 4 y at x+X/2
+// (warps 0-3 and 4-7).  That pairing lets the kernel apply the first radix-2
+// stage of the x transform on the way out (split_out: planes hold
+// a = (s(x) + s(x+X/2))/2 and b = (s(x) - s(x+X/2)) W_X^x/2 in rows x and x+X/2) and
+// undo it on the way in (split_in: s = a +/- W_X^-x b), so the plane kernels
+// work on X/2-row half-planes (their transforms are normalised by the
+// half-plane size).  MODE selects the column work at compile time.
 // ---------------------------------------------------------------------------
-template <class PL, int C>
-__global__ void __launch_bounds__(32 * C) tk_fast(TParams p) {
+enum TMode : int { TM_PLAIN = 0, TM_FLUX = 1, TM_STATS = 2 };
+
+template <class PL, int MODE>
+__global__ void __launch_bounds__(256) tk_fast(TParams p) {
   if (*p.status != 0) return;
+  constexpr int C = 8;
   constexpr int M = PL::N;
   constexpr int N1 = PL::N1;
   constexpr int N2 = PL::N2;
   constexpr int CH = (2 * M + 31) / 32;
+  // column stride: padded line + 2, so the 8 columns of a tile fall in
+  // different shared-memory banks in the pair (k, M-k) phases
+  constexpr int LS = PL::PADDED + 2;
   const int nT = 2 * M;
   extern __shared__ float4 smraw[];
   float2* lines = reinterpret_cast<float2*>(smraw);
-  float2* twM = lines + C * PL::PADDED;
+  float2* stage = lines + C * LS;                       // TM_FLUX only
+  float2* twM = stage + (MODE == TM_FLUX ? C * LS : 0);
   float2* twT = twM + M;
   __shared__ float red_max[C];
 
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int c0 = blockIdx.x * C;
+  const int X = p.X, Y = p.Y, X2 = p.X / 2;
   const int ncols = p.ncols;
+  // tile -> (x, y0); columns of warp w: x + (w>=4)*X2, y0 + (w&3)
+  const int tile = blockIdx.x;
+  const int xq = tile / (Y / 4), y0 = 4 * (tile - xq * (Y / 4));
   for (int i = tid; i < M; i += nthr) twM[i] = p.twM[i];
   for (int i = tid; i <= M; i += nthr) twT[i] = p.tw[i];
+  const float2 wx = p.twX[xq];  // W_X^x of this tile's column pair
 
-  float2* myline = lines + warp * PL::PADDED;
-  const int mycol = c0 + warp;
-  const bool active = mycol < ncols;
+  float2* myline = lines + warp * LS;
+  const int mycol = (xq + (warp >= 4 ? X2 : 0)) * Y + y0 + (warp & 3);
 
   // ---------------- phase 1: input ----------------
   if (p.in_real) {
     __syncthreads();
-    if (active) {
-      const float2* src = reinterpret_cast<const float2*>(p.real_in + (size_t)mycol * nT);
-      for (int j = lane; j < M; j += 32) myline[PL::pos(j)] = src[j];
-    }
+    const float2* src = reinterpret_cast<const float2*>(p.real_in + (size_t)mycol * nT);
+    for (int j = lane; j < M; j += 32) myline[PL::pos(j)] = src[j];
     __syncwarp();
   } else {
     __syncthreads();
     const float inv2M = 0.5f / (float)M;
     const int npairs = M / 2 + 1;
-    for (int it = tid; it < npairs * C; it += nthr) {
-      const int cc = it % C, k = it / C;
-      const int c = c0 + cc;
-      if (c >= ncols) continue;
-      float2* line = lines + cc * PL::PADDED;
+    const size_t colA = (size_t)xq * Y + y0;        // row x
+    const size_t colB = colA + (size_t)X2 * Y;       // row x + X/2
+#pragma unroll 2
+    for (int it = tid; it < npairs * 4; it += nthr) {
+      const int u = it & 3, k = it >> 2;
+      const int k2 = M - k;
+      const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
+      const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
+      const float2* pk = p.spec + (size_t)sk * ncols + u;
+      const float2* pm = p.spec + (size_t)sk2 * ncols + u;
+      float2 xa = pk[colA], xb = pk[colB], ma = pm[colA], mb = pm[colB];
+      if (p.split_in) {
+        const float2 tb = cmulc(xb, wx), tm = cmulc(mb, wx);
+        const float2 a0 = xa, m0 = ma;
+        xa = cadd(a0, tb);
+        xb = csub(a0, tb);
+        ma = cadd(m0, tm);
+        mb = csub(m0, tm);
+      }
+      float2* la = lines + u * LS;
+      float2* lb = lines + (u + 4) * LS;
       if (k == 0) {
-        const float a = p.spec[c].x;                           // DC (imag dropped)
-        const float b = p.spec[(size_t)M * ncols + c].x;       // Nyquist (imag dropped)
-        line[PL::pos(0)] = make_float2((a + b) * inv2M, (a - b) * inv2M);
+        // bins 0 and M: imaginary parts dropped (irfft)
+        la[PL::pos(0)] = make_float2((xa.x + ma.x) * inv2M, (xa.x - ma.x) * inv2M);
+        lb[PL::pos(0)] = make_float2((xb.x + mb.x) * inv2M, (xb.x - mb.x) * inv2M);
       } else {
-        const int k2 = M - k;
-        const int sk = PL::slot_of_freq(k), sk2 = PL::slot_of_freq(k2);
-        const float2 xk = p.spec[(size_t)sk * ncols + c];
-        const float2 xm = p.spec[(size_t)sk2 * ncols + c];
-        const float2 E = make_float2(0.5f * (xk.x + xm.x), 0.5f * (xk.y - xm.y));
-        const float2 D = make_float2(0.5f * (xk.x - xm.x), 0.5f * (xk.y + xm.y));
-        const float2 O = cmulc(D, twT[k]);
-        // Z[k] = E + iO ; Z[M-k] = conj(E) + i conj(O)
-        line[PL::pos(sk)] = make_float2((E.x - O.y) * (2.f * inv2M), (E.y + O.x) * (2.f * inv2M));
-        line[PL::pos(sk2)] = make_float2((E.x + O.y) * (2.f * inv2M), (-E.y + O.x) * (2.f * inv2M));
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          const float2 xk = side ? xb : xa;
+          const float2 xm = side ? mb : ma;
+          float2* line = side ? lb : la;
+          const float2 E = make_float2(0.5f * (xk.x + xm.x), 0.5f * (xk.y - xm.y));
+          const float2 D = make_float2(0.5f * (xk.x - xm.x), 0.5f * (xk.y + xm.y));
+          const float2 O = cmulc(D, twT[k]);
+          // Z[k] = E + iO ; Z[M-k] = conj(E) + i conj(O)
+          line[PL::pos(sk)] = make_float2((E.x - O.y) * (2.f * inv2M), (E.y + O.x) * (2.f * inv2M));
+          line[PL::pos(sk2)] = make_float2((E.x + O.y) * (2.f * inv2M), (-E.y + O.x) * (2.f * inv2M));
+        }
       }
     }
     __syncthreads();
     // inverse four-step on my column: B^-1 then A^-1
-    if (active) {
-      for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, true>(myline, ka);
-      __syncwarp();
-      for (int b = lane; b < N2; b += 32) stepA_inv_smem<PL>(myline, b, twM);
-      __syncwarp();
-    }
+    for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, true>(myline, ka);
+    __syncwarp();
+    for (int b = lane; b < N2; b += 32) stepA_inv_smem<PL>(myline, b, twM);
+    __syncwarp();
   }
 
   // ---------------- phase 2: column work ----------------
   float am = 0.f;
-  if (active) {
+  {
     PaddedColumn<N2> col{reinterpret_cast<float*>(myline)};
-    am = column_phase<CH>(col, mycol, nT, p.op, p.stats != 0);
+    PaddedColumn<N2> stg{reinterpret_cast<float*>(MODE == TM_FLUX ? stage + warp * LS : myline)};
+    ColumnOps op = p.op;
+    if (MODE != TM_FLUX) op.flux = FLUX_NONE;
+    am = column_phase<CH>(col, stg, mycol, nT, op, MODE == TM_STATS);
     if (p.write_real) {
       float2* dst = reinterpret_cast<float2*>(p.real_out + (size_t)mycol * nT);
       for (int j = lane; j < M; j += 32) dst[j] = myline[PL::pos(j)];
     }
   }
-  if (p.stats) {
+  if (MODE == TM_STATS) {
     if (lane == 0) red_max[warp] = am;
     __syncthreads();
     if (tid == 0) {
@@ -119,36 +152,60 @@ __global__ void __launch_bounds__(32 * C) tk_fast(TParams p) {
   if (!p.do_r2c) return;
 
   // ---------------- phase 3: forward real FFT ----------------
-  if (active) {
-    for (int b = lane; b < N2; b += 32) stepA_fwd_smem<PL, false>(myline, b, twM);
-    __syncwarp();
-    for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, false>(myline, ka);
-  }
+  for (int b = lane; b < N2; b += 32) stepA_fwd_smem<PL, false>(myline, b, twM);
+  __syncwarp();
+  for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, false>(myline, ka);
   __syncthreads();
   {
     const int npairs = M / 2 + 1;
-    for (int it = tid; it < npairs * C; it += nthr) {
-      const int cc = it % C, k = it / C;
-      const int c = c0 + cc;
-      if (c >= ncols) continue;
-      const float2* line = lines + cc * PL::PADDED;
-      if (k == 0) {
-        const float2 z = line[PL::pos(0)];
-        p.spec[c] = make_float2(z.x + z.y, 0.f);
-        p.spec[(size_t)M * ncols + c] = make_float2(z.x - z.y, 0.f);
-      } else {
-        const int k2 = M - k;
-        const int sk = PL::slot_of_freq(k), sk2 = PL::slot_of_freq(k2);
-        const float2 zk = line[PL::pos(sk)];
-        const float2 zm = line[PL::pos(sk2)];
-        const float2 E = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-        // O = -i/2 (zk - conj zm)
-        const float2 D = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
-        const float2 O = make_float2(D.y, -D.x);
-        const float2 WO = cmul(O, twT[k]);
-        p.spec[(size_t)sk * ncols + c] = make_float2(E.x + WO.x, E.y + WO.y);
-        p.spec[(size_t)sk2 * ncols + c] = make_float2(E.x - WO.x, -(E.y - WO.y));
+    const size_t colA = (size_t)xq * Y + y0;
+    const size_t colB = colA + (size_t)X2 * Y;
+#pragma unroll 2
+    for (int it = tid; it < npairs * 4; it += nthr) {
+      const int u = it & 3, k = it >> 2;
+      const int k2 = M - k;
+      const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
+      const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
+      float2 ra[2], rb[2];  // [0]: bin k, [1]: bin M-k, for rows x and x+X/2
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const float2* line = lines + (u + 4 * side) * LS;
+        float2 r0, r1;
+        if (k == 0) {
+          const float2 z = line[PL::pos(0)];
+          r0 = make_float2(z.x + z.y, 0.f);
+          r1 = make_float2(z.x - z.y, 0.f);
+        } else {
+          const float2 zk = line[PL::pos(sk)];
+          const float2 zm = line[PL::pos(sk2)];
+          const float2 E = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+          const float2 D = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
+          const float2 O = make_float2(D.y, -D.x);  // -i/2 (zk - conj zm)
+          const float2 WO = cmul(O, twT[k]);
+          r0 = make_float2(E.x + WO.x, E.y + WO.y);
+          r1 = make_float2(E.x - WO.x, -(E.y - WO.y));
+        }
+        if (side == 0) { ra[0] = r0; ra[1] = r1; }
+        else { rb[0] = r0; rb[1] = r1; }
       }
+      if (p.split_out) {
+        // a = (s(x) + s(x+X/2))/2, b = (s(x) - s(x+X/2)) W_X^x / 2: the input
+        // side s = a +/- W_X^-x b then inverts it exactly
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const float2 a = cscale(cadd(ra[j], rb[j]), 0.5f);
+          const float2 b = cmul(csub(ra[j], rb[j]), make_float2(0.5f * wx.x, 0.5f * wx.y));
+          ra[j] = a;
+          rb[j] = b;
+        }
+      }
+      float2* so = p.spec_out ? p.spec_out : p.spec;
+      float2* pk = so + (size_t)sk * ncols + u;
+      float2* pm = so + (size_t)sk2 * ncols + u;
+      pk[colA] = ra[0];
+      pk[colB] = rb[0];
+      pm[colA] = ra[1];
+      pm[colB] = rb[1];
     }
   }
 }
@@ -166,6 +223,7 @@ __global__ void __launch_bounds__(128) tk_generic(TParams p, GenPlan pl) {
   float2* A = reinterpret_cast<float2*>(smraw);
   float2* B = A + C * nT;
   float2* tw = B + C * nT;
+  float* stg_base = reinterpret_cast<float*>(tw + nT);  // KT stage-1 values [C][nT]
   __shared__ float red_max[C];
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -209,7 +267,8 @@ __global__ void __launch_bounds__(128) tk_generic(TParams p, GenPlan pl) {
   float am = 0.f;
   if (active) {
     PlainColumn col{re + warp * nT};
-    am = column_phase<CH>(col, mycol, nT, p.op, p.stats != 0);
+    PlainColumn stg{stg_base + warp * nT};
+    am = column_phase<CH>(col, stg, mycol, nT, p.op, p.stats != 0);
     if (p.write_real) {
       for (int t = lane; t < nT; t += 32) p.real_out[(size_t)mycol * nT + t] = col.get(t);
     }
@@ -240,28 +299,36 @@ __global__ void __launch_bounds__(128) tk_generic(TParams p, GenPlan pl) {
   for (int it = tid; it < C * F; it += nthr) {
     const int cc = it % C, f = it / C;
     const int c = c0 + cc;
-    if (c < ncols) p.spec[(size_t)f * ncols + c] = res[cc * nT + f];
+    if (c < ncols) (p.spec_out ? p.spec_out : p.spec)[(size_t)f * ncols + c] = res[cc * nT + f];
   }
 }
 
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
-template <int M>
-static int launch_fast_t(const TParams& p, cudaStream_t st) {
+template <int M, int MODE>
+static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   using PL = FastPlan<M>;
   constexpr int C = 8;
-  const size_t smem = (size_t)(C * PL::PADDED + M + M + 1) * sizeof(float2);
+  constexpr int LS = PL::PADDED + 2;
+  const size_t smem = (size_t)((MODE == TM_FLUX ? 2 : 1) * C * LS + M + M + 1) * sizeof(float2);
   static bool attr_done = false;
   if (!attr_done) {
-    if (cudaFuncSetAttribute(tk_fast<PL, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(tk_fast<PL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return ASG_ERR_CUDA;
     attr_done = true;
   }
-  const int grid = (p.ncols + C - 1) / C;
-  tk_fast<PL, C><<<grid, 32 * C, smem, st>>>(p);
+  const int grid = (p.X / 2) * (p.Y / 4);
+  tk_fast<PL, MODE><<<grid, 32 * C, smem, st>>>(p);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
+template <int M>
+static int launch_fast_t(const TParams& p, cudaStream_t st) {
+  if (p.stats) return launch_fast_t_mode<M, TM_STATS>(p, st);
+  if (p.op.flux != FLUX_NONE) return launch_fast_t_mode<M, TM_FLUX>(p, st);
+  return launch_fast_t_mode<M, TM_PLAIN>(p, st);
 }
 
 bool asg_t_fast_supported(int nT) {
@@ -275,7 +342,9 @@ bool asg_t_fast_supported(int nT) {
 }
 
 // generic: C = 4 columns of nT complex, ping-pong
-size_t asg_t_generic_smem(int nT) { return (size_t)(2 * 4 * nT + nT) * sizeof(float2); }
+size_t asg_t_generic_smem(int nT) {
+  return (size_t)(2 * 4 * nT + nT) * sizeof(float2) + (size_t)4 * nT * sizeof(float);
+}
 
 template <int CH>
 static int launch_generic_t_ch(const TParams& p, const GenPlan& pl, cudaStream_t st) {

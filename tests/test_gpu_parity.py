@@ -157,20 +157,35 @@ FAST_CASES = {
     "lie_water_96": ((96, 96, 192), dict(useSplitStep=False, alpha0=-1.0), 3e6, 8),
     "kt_obl_32x64": ((32, 64, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
                      6e6, 8),
+    # half-plane (split-x) kernels with the beam-obliquity power pass
+    "kt_obl_split_64x128": ((64, 128, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
+                            6e6, 6),
+    # half-plane kernels, Lie, water, screens and sources through the epilogue pass
+    "lie_screens_sources_split": ((64, 128, 128), dict(useSplitStep=False, alpha0=-1.0), 2e6, 8,
+                                  dict(zs=[3.0e-4, 7.5e-4, 1.1e-3], amp=[False, True, True]),
+                                  dict(zs=[1.0e-4, 5.0e-4, 1.6e-3])),
+    # configs[0]-like grid at full size (128^2 x 256) for a few steps
+    "c1_grid_tvd_wendland": ((128, 128, 256), dict(fluxScheme="rusanov", boundaryProfile="wendland",
+                                                   dX=3.08e-4, dY=3.08e-4, f0=1e6), 4e5, 6),
 }
 
 
 @pytest.mark.parametrize("name", list(FAST_CASES))
 def test_fast_solve_vs_oracle(lib, name):
-    shape, kwx, p0, nsteps = FAST_CASES[name]
+    shape, kwx, p0, nsteps = FAST_CASES[name][:4]
     nX, nY, nT = shape
     kw = dict(S.BASE)
     kw.update(kwx)
     kw["propDist"] = nsteps * kw["dZmin"]
     u0 = S.piston_field(nX, nY, nT, kw["dX"], kw["dY"], kw["dT"], kw["f0"], p0,
                         radius=0.35 * nX * kw["dX"], focus=8e-3)
-    res = _gpu_solve(u0, kw, {})
-    ref = O.solve(u0, oracle_params(kw), "fp64")
+    ex = {}
+    if len(FAST_CASES[name]) > 4:
+        scr, src = FAST_CASES[name][4:6]
+        ex["phaseScreens"] = S._screens(nX, nY, 5, scr["zs"], scr["amp"])
+        ex["sourcePlanes"] = S._sources(nX, nY, nT, kw["dT"], kw["f0"], src["zs"], 9)
+    res = _gpu_solve(u0, kw, ex)
+    ref = O.solve(u0, oracle_params(kw, ex), "fp64")
     for k, a, r in zip(KEYS, res, ref):
         if k == "zaxis":
             np.testing.assert_array_equal(a, r)
