@@ -98,9 +98,12 @@ static void roots(int n, std::vector<float2>& out) {
   }
 }
 
+static constexpr int L2_MAX_CLUSTERS = 32;
+
 // four-step slot order of a fast line of length n (n = n1*n2)
 static void fast_factors(int n, int* n1, int* n2) {
   switch (n) {
+    case 32: *n1 = 4; *n2 = 8; break;
     case 64: *n1 = 8; *n2 = 8; break;
     case 96: *n1 = 8; *n2 = 12; break;
     case 128: *n1 = 8; *n2 = 16; break;
@@ -177,7 +180,10 @@ struct asg_plan {
   int X, Y, T, ncols, F, M;
   bool tfast, xyfast;
   bool split;  // half-plane transforms: the column pass applies the first radix-2 x stage
+  bool l2;     // plane kernel with the x exchange through an L2-resident scratch
   int G, nsub;
+  float2* l2_scratch = nullptr;
+  int* l2_cls_x = nullptr;
   float2* spec2 = nullptr;  // whole-plane output of the epilogue pass
   GenPlan gp_t, gp_x, gp_y;
   cudaStream_t st;
@@ -295,7 +301,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.map);
     cudaFree(s.val);
   }
-  void* ptrs[] = {p->spec, p->spec2, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->spec, p->spec2, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
@@ -318,7 +324,8 @@ static int upload_roots() {
   roots(192, w192);
   roots(64, w64);
   if (asg_roots_upload_t(w192.data(), w64.data()) != 0 ||
-      asg_roots_upload_xy(w192.data(), w64.data()) != 0)
+      asg_roots_upload_xy(w192.data(), w64.data()) != 0 ||
+      asg_roots_upload_l2(w192.data(), w64.data()) != 0)
     return fail(ASG_ERR_CUDA, "upload of the constant root tables failed");
   g_roots_done = true;
   return ASG_OK;
@@ -336,12 +343,13 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   p->M = T / 2;
   p->N = cfg->beta / (2.0 * cfg->c0 * cfg->c0 * cfg->c0 * cfg->rho0);
   p->tfast = asg_t_fast_supported(T) && X % 2 == 0 && Y % 4 == 0;
-  int Gs = 0;
-  p->split = p->tfast && asg_xy_split_supported(X, Y, &Gs);
+  int Gs = 0, Gl = 0;
+  p->l2 = p->tfast && asg_xy_l2_supported(X, Y, 2, &Gl);
+  p->split = p->l2 || (p->tfast && asg_xy_split_supported(X, Y, &Gs));
   p->xyfast = p->split || asg_xy_fast_supported(X, Y, &p->G);
   p->nsub = 1;
   if (p->split) {
-    p->G = Gs;
+    p->G = p->l2 ? Gl : Gs;
     p->nsub = 2;
   }
   if (!p->xyfast) {
@@ -439,6 +447,23 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   const size_t nspec = (size_t)p->F * p->ncols;
   CKS(dalloc(&p->spec, nspec));
   if (p->split) CKS(dalloc(&p->spec2, nspec));
+  if (p->l2) {
+    // scratch for up to L2_MAX_CLUSTERS clusters, two half-planes each
+    const int Xs = X / 2;
+    CKS(dalloc(&p->l2_scratch, (size_t)L2_MAX_CLUSTERS * 2 * Xs * Y));
+    int n1, n2;
+    fast_factors(Xs, &n1, &n2);
+    std::vector<int> cl(2 * Xs);
+    for (int h = 0; h < 2; ++h)
+      for (int sl = 0; sl < Xs; ++sl) {
+        const int kxs = (sl / n2) + n1 * (sl % n2);  // bin of the Xs-point FFT in slot sl
+        const int kx = 2 * kxs + h;
+        const int i = (kx + X / 2) % X;
+        cl[h * Xs + sl] = i < X - 1 - i ? i : X - 1 - i;
+      }
+    CKS(dalloc(&p->l2_cls_x, 2 * Xs));
+    CKS(h2d(p->l2_cls_x, cl.data(), 2 * Xs, p->st));
+  }
   CKS(dalloc(&p->real, (size_t)p->ncols * T));
   std::vector<float2> w;
   roots(T, w);
@@ -786,6 +811,9 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.screen_fscale = p->screen_fscale;
   x.obl_table = p->obl_tab;
   x.power_acc = p->power_acc;
+  x.l2_scratch = p->l2_scratch;
+  x.l2_cls_x = p->l2_cls_x;
+  x.l2_max_clusters = L2_MAX_CLUSTERS;
   return x;
 }
 
@@ -795,6 +823,7 @@ static int run_t(asg_plan* p, const TParams& t, int kind = ASG_K_OTHER) {
 }
 static int run_xy(asg_plan* p, const XYParams& x, int kind = ASG_K_OTHER) {
   KScope k(p, kind);
+  if (p->l2 && x.epi == 0 && x.nscreens == 0) return asg_launch_xy_l2(x, p->st);
   return asg_launch_xy(x, p->xyfast, p->gp_x, p->gp_y, p->st);
 }
 

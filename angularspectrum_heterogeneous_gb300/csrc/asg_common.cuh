@@ -176,6 +176,7 @@ struct LinePlan {
 
 // Fast sizes: N -> (N1, N2)
 template <int N> struct FastPlan;
+template <> struct FastPlan<32> : LinePlan<4, 8> {};
 template <> struct FastPlan<64> : LinePlan<8, 8> {};
 template <> struct FastPlan<96> : LinePlan<8, 12> {};
 template <> struct FastPlan<128> : LinePlan<8, 16> {};

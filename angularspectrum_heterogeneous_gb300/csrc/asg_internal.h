@@ -87,9 +87,17 @@ struct XYParams {
   unsigned* status;
   int* status_step;
   const int* step;
+  // L2-exchange plane kernel
+  float2* l2_scratch;      // [clusters][2][Xs][Y]
+  const int* l2_cls_x;     // [nsub][Xs] class of each x slot of the Xs-point FFT
+  int l2_buf_elems;        // set by the launcher
+  int l2_max_clusters;     // clusters the scratch was sized for
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);
+// L2-exchange plane kernel (asg_xyl2.cu)
+bool asg_xy_l2_supported(int X, int Y, int nsub, int* G_out);
+int asg_launch_xy_l2(const XYParams& p, cudaStream_t st);
 // half-plane kernels (rows x < X/2 and x >= X/2 transformed separately)
 bool asg_xy_split_supported(int X, int Y, int* G_out);
 int asg_launch_epilogue_pass(const XYParams& p, const float2* src, float2* dst, int split,
@@ -126,3 +134,4 @@ int asg_launch_transpose(const float* in, float* out, int nz, int ncols, cudaStr
 
 int asg_roots_upload_t(const float2* w192, const float2* w64);
 int asg_roots_upload_xy(const float2* w192, const float2* w64);
+int asg_roots_upload_l2(const float2* w192, const float2* w64);

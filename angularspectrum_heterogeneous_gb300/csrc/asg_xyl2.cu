@@ -1,0 +1,352 @@
+// Plane kernel with the x exchange through an L2-resident scratch.
+//
+// A thread-block cluster of G CTAs owns one (half-)plane of Xs x Y modes at a
+// time (persistent, planes strided by the cluster count):
+//   1. each CTA loads R rows (cp.async, prefetched during the previous
+//      plane), runs the forward y FFT in shared memory and writes the rows to
+//      the cluster's scratch buffer in global memory (it stays in L2);
+//   2. cluster barrier; each CTA takes Yc = Y/G y-columns of all Xs rows from
+//      the scratch, runs the forward x FFT, the per-mode multiplier and the
+//      inverse x FFT (the middle four-step stage, multiplier and its inverse
+//      never leave registers), and writes the columns back;
+//   3. cluster barrier; each CTA reads its rows back, runs the inverse y FFT
+//      and stores the rows to HBM.
+// The scratch is double-buffered between consecutive planes, so a cluster
+// needs only the two barriers per plane.  Shared memory holds either R rows
+// or Xs x Yc columns, both about 64 KB for 512 x 512 planes split in halves,
+// so two CTAs share an SM.
+//
+// Reference semantics are those of the plane kernels in asg_xykernel.cu
+// (angular_spectrum_solver.py :649-655, :667-685, :630-643).
+#include <cooperative_groups.h>
+
+#include "asg_internal.h"
+
+namespace cg = cooperative_groups;
+
+ASG_DEFINE_ROOT_UPLOADER(asg_roots_upload_l2)
+
+namespace {
+
+ASG_DEV void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+ASG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+ASG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+ASG_DEV bool is_dc_or_nyq_l2(int f, int nT) { return f == 0 || 2 * f == nT; }
+
+ASG_DEV bool l2_should_skip(const XYParams& p) {
+  if (*((volatile const unsigned*)p.status) != 0u) return true;
+  if (p.check_stability) {
+    const float m = __uint_as_float(*p.max_cur);
+    const bool nan = (m != m) || isinf(m);
+    const bool bad = nan || (p.stab_coef * (double)m > p.stab_thr);
+    if (bad) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (atomicCAS(p.status, 0u, (unsigned)(nan ? -ASG_ERR_NAN : -ASG_ERR_STABILITY)) == 0u)
+          *p.status_step = *p.step;
+      }
+      return true;
+    }
+  }
+  return false;
+}
+
+}  // namespace
+
+template <class PY, class PX, int R, int NT>
+__global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
+  constexpr int Y = PY::N, RS = PY::PADDED;
+  constexpr int Xs = PX::N;
+  constexpr int NW = NT / 32;
+  const int G = p.G;                 // = Xs / R
+  const int Yc = Y / G;              // y-columns per CTA in stage 2
+  const int TS = Yc;                 // row stride of the column tile (complex): lanes run
+                                     // along c, so the strided x accesses are conflict free
+  extern __shared__ float4 smraw[];
+  float2* buf = reinterpret_cast<float2*>(smraw);       // rows [R][RS] or tile [Xs][TS]
+  __shared__ float red[2][NW];
+
+  const int nbuf = p.l2_buf_elems;   // max(R*RS, Xs*TS), set by the host
+  float2* tw_y = buf + nbuf;
+  float2* tw_x = tw_y + Y;
+  int* clsy = reinterpret_cast<int*>(tw_x + Xs);
+  int* clsx = clsy + Y;               // [nsub][Xs] by x slot of the Xs-point FFT
+
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (G > 1) ? (int)cl.block_rank() : 0;
+  const int cid = blockIdx.x / G, ncl = gridDim.x / G;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nsub = p.nsub;
+  const int nq = p.nplanes * nsub;
+  if (l2_should_skip(p)) return;
+
+  for (int i = tid; i < Y; i += NT) {
+    tw_y[i] = p.twY[i];
+    clsy[i] = p.cls_y[i];
+  }
+  for (int i = tid; i < Xs; i += NT) tw_x[i] = p.twX[i * nsub];  // W_Xs^i
+  for (int i = tid; i < nsub * Xs; i += NT) clsx[i] = p.l2_cls_x[i];
+  float2* scratch0 = p.l2_scratch + (size_t)cid * 2 * Xs * Y;
+
+  auto zero_plane = [&](int q) {
+    return p.zero_dc_nyq && is_dc_or_nyq_l2(p.f_of_plane[q / nsub], p.nT);
+  };
+  auto sub_base = [&](int q) {
+    const int plane = q / nsub, h = q - (q / nsub) * nsub;
+    return p.spec + ((size_t)plane * p.X + (size_t)h * Xs) * Y;
+  };
+  auto prefetch_row = [&](int q, int r) {
+    const float2* g = sub_base(q) + (size_t)(rank * R + r) * Y;
+    float2* d = buf + r * RS;
+    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
+  };
+  int issued = -1;
+  int par = 0;
+
+  for (int q = cid; q < nq; q += ncl) {
+    const int plane = q / nsub, h = q - (q / nsub) * nsub;
+    if (zero_plane(q)) {
+      float4* g4 = reinterpret_cast<float4*>(sub_base(q) + (size_t)rank * R * Y);
+      for (int i = tid; i < R * Y / 2; i += NT) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    float2* S = scratch0 + (size_t)par * Xs * Y;
+    par ^= 1;
+    if (issued != q) {
+      for (int r = warp; r < R; r += NW) prefetch_row(q, r);
+      cp_async_commit();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- 1. forward y FFT on my rows, rows -> scratch (slot order) ----
+    for (int r = warp; r < R; r += NW) {
+      float2* row = buf + r * RS;
+      for (int b = lane; b < PY::N2; b += 32) stepA_fwd_smem<PY, false>(row, b, tw_y);
+      __syncwarp();
+      for (int ka = lane; ka < PY::N1; ka += 32) stepB_smem<PY, false>(row, ka);
+      __syncwarp();
+      float4* dst = reinterpret_cast<float4*>(S + (size_t)(rank * R + r) * Y);
+      for (int s2 = lane; s2 < Y / 2; s2 += 32)
+        dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
+    }
+    __threadfence();  // scratch writes visible to the other CTAs of the cluster
+    if (G > 1) cl.sync();
+    else __syncthreads();
+
+    // ---- 2. columns [rank*Yc, +Yc) of all Xs rows: x FFT, multiplier, inverse ----
+    {
+      const int c0 = rank * Yc;
+      // tile[x][c], row stride TS
+      for (int i = tid; i < Xs * Yc / 2; i += NT) {
+        const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
+        cp_async16(buf + x * TS + c2, S + (size_t)x * Y + c0 + c2);
+      }
+      cp_async_commit();
+      cp_async_wait_all();
+      __syncthreads();
+      // step A (forward): task (b, c), elements x = b + N2x*a
+      for (int it = tid; it < PX::N2 * Yc; it += NT) {
+        const int b = it / Yc, c = it - b * Yc;
+        float2 v[PX::N1];
+#pragma unroll
+        for (int a = 0; a < PX::N1; ++a) v[a] = buf[(b + PX::N2 * a) * TS + c];
+        dft<PX::N1, false>(v);
+        buf[b * TS + c] = v[0];
+#pragma unroll
+        for (int ka = 1; ka < PX::N1; ++ka) buf[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x[b * ka]);
+      }
+      __syncthreads();
+      float psum = 0.f, pden = 0.f;
+      // step B forward, multiplier, step B inverse: task (ka, c), slots kb + N2x*ka
+      for (int it = tid; it < PX::N1 * Yc; it += NT) {
+        const int ka = it / Yc, c = it - ka * Yc;
+        float2 v[PX::N2];
+#pragma unroll
+        for (int b = 0; b < PX::N2; ++b) v[b] = buf[(b + PX::N2 * ka) * TS + c];
+        dft<PX::N2, false>(v);
+        const int cy = clsy[c0 + c];
+        const int* cxh = clsx + h * Xs;
+        if (p.power_only) {
+          const float* ot = p.obl_table + (size_t)plane * p.ncx * p.ncy + cy;
+#pragma unroll
+          for (int kb = 0; kb < PX::N2; ++kb) {
+            const float o = ot[(size_t)cxh[kb + PX::N2 * ka] * p.ncy];
+            const float P = v[kb].x * v[kb].x + v[kb].y * v[kb].y;
+            psum = fmaf(P, o, psum);
+            pden += (o > 0.f) ? P : 0.f;
+          }
+          continue;
+        }
+        if (p.table != nullptr) {
+          const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + cy;
+#pragma unroll
+          for (int kb = 0; kb < PX::N2; ++kb)
+            v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
+        } else {
+          const float nrm = 1.0f / ((float)Xs * (float)Y);
+#pragma unroll
+          for (int kb = 0; kb < PX::N2; ++kb) v[kb] = cscale(v[kb], nrm);
+        }
+        dft<PX::N2, true>(v);
+#pragma unroll
+        for (int b = 0; b < PX::N2; ++b) buf[(b + PX::N2 * ka) * TS + c] = v[b];
+      }
+      if (p.power_only) {
+        psum = warp_sum(psum);
+        pden = warp_sum(pden);
+        if (lane == 0) {
+          red[0][warp] = psum;
+          red[1][warp] = pden;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double a = 0.0, b = 0.0;
+          for (int w = 0; w < NW; ++w) {
+            a += (double)red[0][w];
+            b += (double)red[1][w];
+          }
+          atomicAdd(p.power_acc, a);
+          atomicAdd(p.power_acc + 1, b);
+        }
+        // no CTA reuses the scratch before every CTA has read it
+        if (G > 1) cl.sync();
+        else __syncthreads();
+        continue;
+      }
+      __syncthreads();
+      // step A inverse: task (b, c)
+      for (int it = tid; it < PX::N2 * Yc; it += NT) {
+        const int b = it / Yc, c = it - b * Yc;
+        float2 v[PX::N1];
+        v[0] = buf[b * TS + c];
+#pragma unroll
+        for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(buf[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
+        dft<PX::N1, true>(v);
+#pragma unroll
+        for (int a = 0; a < PX::N1; ++a) buf[(b + PX::N2 * a) * TS + c] = v[a];
+      }
+      __syncthreads();
+      for (int i = tid; i < Xs * Yc / 2; i += NT) {
+        const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
+        *reinterpret_cast<float4*>(S + (size_t)x * Y + c0 + c2) =
+            *reinterpret_cast<const float4*>(buf + x * TS + c2);
+      }
+    }
+    __threadfence();
+    if (G > 1) cl.sync();
+    else __syncthreads();
+
+    // ---- 3. my rows back from the scratch, inverse y FFT, store ----
+    for (int r = warp; r < R; r += NW) {
+      const float4* srcr = reinterpret_cast<const float4*>(S + (size_t)(rank * R + r) * Y);
+      float2* row = buf + r * RS;
+      for (int s2 = lane; s2 < Y / 2; s2 += 32)  // L2 only: other CTAs wrote these
+        *reinterpret_cast<float4*>(row + PY::pos(2 * s2)) = __ldcg(srcr + s2);
+    }
+    int qn = q + ncl;
+    while (qn < nq && zero_plane(qn)) qn += ncl;
+    const bool pref = qn < nq;
+    __syncthreads();
+    float2* gbase = sub_base(q) + (size_t)rank * R * Y;
+    for (int r = warp; r < R; r += NW) {
+      float2* row = buf + r * RS;
+      float2* grow = gbase + (size_t)r * Y;
+      for (int ka = lane; ka < PY::N1; ka += 32) stepB_smem<PY, true>(row, ka);
+      __syncwarp();
+      for (int b = lane; b < PY::N2; b += 32) {
+        float2 v[PY::N1];
+        v[0] = row[PY::pos(b)];
+#pragma unroll
+        for (int ka = 1; ka < PY::N1; ++ka) v[ka] = cmulc(row[PY::pos(b + PY::N2 * ka)], tw_y[b * ka]);
+        dft<PY::N1, true>(v);
+#pragma unroll
+        for (int a = 0; a < PY::N1; ++a) grow[b + PY::N2 * a] = v[a];
+      }
+      __syncwarp();
+      if (pref) prefetch_row(qn, r);
+    }
+    if (pref) {
+      cp_async_commit();
+      issued = qn;
+    }
+  }
+  cp_async_wait_all();
+}
+
+// ---------------------------------------------------------------------------
+bool asg_xy_l2_supported(int X, int Y, int nsub, int* G_out) {
+  if (X % nsub) return false;
+  const int Xs = X / nsub;
+  int ok = 0;
+  switch (Y) {
+    case 128: ok = (Xs == 32 || Xs == 64); break;
+    case 192: ok = (Xs == 96); break;
+    case 256: ok = (Xs == 128); break;
+    case 384: ok = (Xs == 192); break;
+    case 512: ok = (Xs == 256); break;
+    default: ok = 0;
+  }
+  if (!ok) return false;
+  const int G = Xs / 16;
+  if (G < 1 || G > 16 || Y % G) return false;
+  if (G_out) *G_out = G;
+  return true;
+}
+
+template <int Yn, int Xn>
+static int launch_l2(const XYParams& pin, cudaStream_t st) {
+  using PY = FastPlan<Yn>;
+  using PX = FastPlan<Xn>;
+  constexpr int R = 16, NT = 256;
+  XYParams p = pin;
+  const int Yc = Yn / p.G;
+  const int nbuf = (R * PY::PADDED > Xn * Yc) ? R * PY::PADDED : Xn * Yc;
+  p.l2_buf_elems = nbuf;
+  const size_t smem = (size_t)(nbuf + Yn + Xn) * sizeof(float2) + (size_t)(Yn + 2 * Xn) * sizeof(int);
+  auto kern = xy_l2<PY, PX, R, NT>;
+  static int max_clusters = -1, cached_G = -1;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = p.G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (max_clusters < 0 || cached_G != p.G) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return ASG_ERR_CUDA;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cfg.gridDim = dim3(p.G * 1024, 1, 1);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) n = 1;
+    max_clusters = n;
+    cached_G = p.G;
+  }
+  const int nq = p.nplanes * p.nsub;
+  int ncl = max_clusters < nq ? max_clusters : nq;
+  if (ncl > p.l2_max_clusters) ncl = p.l2_max_clusters;
+  cfg.gridDim = dim3(p.G * ncl, 1, 1);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
+  return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
+int asg_launch_xy_l2(const XYParams& p, cudaStream_t st) {
+  const int Xs = p.X / p.nsub;
+  switch (p.Y) {
+    case 128: return Xs == 32 ? launch_l2<128, 32>(p, st) : launch_l2<128, 64>(p, st);
+    case 192: return launch_l2<192, 96>(p, st);
+    case 256: return launch_l2<256, 128>(p, st);
+    case 384: return launch_l2<384, 192>(p, st);
+    case 512: return launch_l2<512, 256>(p, st);
+    default: return ASG_ERR_SHAPE;
+  }
+}
