@@ -116,7 +116,8 @@ ASG_DEV float kt_fh(float um, float up) {
   if (small) {
     return 0.5f * (fm + fp) - 0.5f * fmaxf(fabsf(um), fabsf(up)) * (up - um);
   }
-  return (ap * fm - am * fp - ap * am * (up - um)) / den;
+  // den >= 1e-14 here: the approximate quotient (2 ulp) is safe
+  return __fdividef(ap * fm - am * fp - ap * am * (up - um), den);
 }
 
 // ---------------------------------------------------------------------------
@@ -208,6 +209,73 @@ ASG_DEV void kt_column_step(const Col& col, const Col& stg, int nT, float ndt, f
   __syncwarp(mask);
 }
 
+// Chunked variant of the KT step: lane l owns samples [l*CH, (l+1)*CH) and keeps
+// its window, stage-1 values and right-hand sides in registers (faster when
+// CH <= 32; the shuffle variant above is used for longer columns).
+// rhs of the KT scheme at the lane's CH points from a window of CH+4 values
+template <int CH, bool MC>
+ASG_DEV void kt_rhs_window(const float (&w)[CH + 4], int t0, int nT, float ndt, float (&rhs)[CH]) {
+  // slopes at window positions 1..CH+2  (t0-1 .. t0+CH); zero at the column ends
+  float s[CH + 2];
+#pragma unroll
+  for (int i = 0; i < CH + 2; ++i) {
+    int t = t0 - 1 + i;
+    s[i] = (t >= 1 && t < nT - 1) ? kt_slope<MC>(w[i], w[i + 1], w[i + 2]) : 0.f;
+  }
+  // interface fluxes at t+1/2 for t = t0-1 .. t0+CH-1
+  float fh[CH + 1];
+#pragma unroll
+  for (int i = 0; i < CH + 1; ++i) {
+    float um = w[i + 1] + 0.5f * s[i];
+    float up = w[i + 2] - 0.5f * s[i + 1];
+    fh[i] = kt_fh(um, up);
+  }
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    rhs[i] = (t >= 1 && t < nT - 1) ? (-ndt * (fh[i + 1] - fh[i])) : 0.f;
+  }
+}
+
+template <int CH, bool MC, class Col>
+ASG_DEV void load_window4(const Col& col, int t0, int nT, float (&w)[CH + 4]) {
+#pragma unroll
+  for (int i = 0; i < CH + 4; ++i) {
+    int t = t0 - 2 + i;
+    w[i] = (t >= 0 && t < nT) ? col.get(t) : 0.f;
+  }
+}
+
+// one SSP-RK2 KT step of size dz on the column
+template <int CH, bool MC, class Col>
+ASG_DEV void kt_column_step_chunk(const Col& col, int nT, float ndt, float dz, unsigned mask) {
+  const int lane = threadIdx.x & 31;
+  const int t0 = lane * CH;
+  float w[CH + 4];
+  load_window4<CH, MC>(col, t0, nT, w);
+  float u[CH], rhs[CH];
+#pragma unroll
+  for (int i = 0; i < CH; ++i) u[i] = w[i + 2];
+  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
+  __syncwarp(mask);
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    if (t < nT) col.set(t, u[i] + dz * rhs[i]);  // stage1
+  }
+  __syncwarp(mask);
+  load_window4<CH, MC>(col, t0, nT, w);
+  kt_rhs_window<CH, MC>(w, t0, nT, ndt, rhs);
+  __syncwarp(mask);
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    int t = t0 + i;
+    float s1 = w[i + 2];
+    if (t < nT) col.set(t, 0.5f * u[i] + 0.5f * (s1 + dz * rhs[i]));
+  }
+  __syncwarp(mask);
+}
+
 template <class Col>
 ASG_DEV float column_absmax(const Col& col, int nT) {
   const int lane = threadIdx.x & 31;
@@ -259,8 +327,13 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
       }
       float dzs = op.dz / (float)nsub;
       for (int k = 0; k < nsub; ++k) {
-        if (op.flux == FLUX_KT_MC) kt_column_step<true>(col, stg, nT, ndt, dzs, mask);
-        else kt_column_step<false>(col, stg, nT, ndt, dzs, mask);
+        if constexpr (CH <= 32) {
+          if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(col, nT, ndt, dzs, mask);
+          else kt_column_step_chunk<CH, false>(col, nT, ndt, dzs, mask);
+        } else {
+          if (op.flux == FLUX_KT_MC) kt_column_step<true>(col, stg, nT, ndt, dzs, mask);
+          else kt_column_step<false>(col, stg, nT, ndt, dzs, mask);
+        }
       }
     }
   }

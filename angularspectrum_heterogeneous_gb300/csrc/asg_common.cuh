@@ -1,8 +1,6 @@
 // Shared device helpers for the angular-spectrum march kernels (sm_103a).
 //
-// Complex numbers are float2 (x = re, y = im).  The packed Blackwell FP32x2
-// instructions (FADD2/FMUL2/FFMA2) are used for complex arithmetic, which
-// halves the FP32 instruction count of the FFT butterflies.
+// Complex numbers are float2 (x = re, y = im).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -12,8 +10,11 @@
 #define ASG_DEV __device__ __forceinline__
 
 // ---------------------------------------------------------------------------
-// complex arithmetic
+// complex arithmetic.  ASG_PACKED_F32X2 selects the Blackwell FP32x2
+// instructions (FADD2/FMUL2/FFMA2); the scalar form is the default (fewer
+// register-pair moves for the twiddle products).
 // ---------------------------------------------------------------------------
+#ifdef ASG_PACKED_F32X2
 ASG_DEV float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 ASG_DEV float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 ASG_DEV float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
@@ -27,6 +28,17 @@ ASG_DEV float2 cmulc(float2 a, float2 b) {
   float2 t = __fmul2_rn(make_float2(a.x, a.x), make_float2(b.x, -b.y));
   return __ffma2_rn(make_float2(a.y, a.y), make_float2(b.y, b.x), t);
 }
+#else
+ASG_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+ASG_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+ASG_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+ASG_DEV float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+ASG_DEV float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+#endif
 ASG_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
