@@ -621,3 +621,83 @@ def solve(initial_field, p: OracleParams, precision="fp32", per_step_callback=No
         cc += 1
     return (np.array(u), pnp[:, :, :cc], ppp[:, :, :cc], pI[:, :, :cc], pIl[:, :, :cc],
             np.cumsum(zvec[:cc]), pax[:, :cc])
+
+
+# ---------------------------------------------------------------------------
+# Step-by-step runner with the same arithmetic as solve(): operators are built
+# once (untimed) and march steps are timed separately -- the CPU baseline.
+# ---------------------------------------------------------------------------
+class OracleMarch:
+    """March state for timing: ``build()`` then ``step()`` repeatedly.
+
+    Only regular steps (no partial last step, screens or sources); the step
+    body is the one of :func:`solve` (``:1413-1536``)."""
+
+    def __init__(self, initial_field, p: OracleParams, precision="fp32"):
+        self.p = p
+        self.rdt = np.float64 if precision == "fp64" else np.float32
+        self.cdt = np.complex128 if precision == "fp64" else np.complex64
+        self.u = np.array(initial_field, dtype=self.rdt)
+        self.nX, self.nY, self.nT = self.u.shape
+        self.N = p.beta / (2 * p.c0 ** 3 * p.rho0)
+        self.dz = max(p.dZmin, min(p.stabilityRecoveryFactor * p.dT /
+                                   (float(np.max(np.abs(self.u))) * self.N + 1e-30), p.dZmin))
+
+    def build(self):
+        p, nX, nY, nT, dz = self.p, self.nX, self.nY, self.nT, self.dz
+        nf = nT // 2 + 1
+        if p.useSplitStep:
+            self.H = propagator(nX, nY, nT, p.dX, p.dY, dz, p.dT, p.c0, p.useAdaptiveFiltering,
+                                p.freqFilterThreshold, p.adaptiveFilterStrength,
+                                half=True).astype(self.cdt)
+            _, ablh = boundary_layer(nX, nY, nT, p.boundaryFactor, p.boundaryProfile,
+                                     p.useBoundaryLayer)
+            self.abl = ablh.astype(self.rdt)
+            _, afh = atten_filters(p, nX, nY, nT, dz)
+            self.af = afh[:, :, :nf].astype(self.cdt)
+        else:
+            self.H = propagator(nX, nY, nT, p.dX, p.dY, dz, p.dT, p.c0, p.useAdaptiveFiltering,
+                                p.freqFilterThreshold, p.adaptiveFilterStrength).astype(self.cdt)
+            abl, _ = boundary_layer(nX, nY, nT, p.boundaryFactor, p.boundaryProfile,
+                                    p.useBoundaryLayer)
+            self.abl = abl.astype(self.rdt)
+            af, _ = atten_filters(p, nX, nY, nT, dz)
+            self.af = af[:, :, :nf].astype(self.cdt)
+        self.fw = freq_weighted_mask(nX, nY, nT, p.dT, p.f0, p.boundaryFactor,
+                                     p.boundaryProfile).astype(self.rdt) \
+            if p.useFreqWeightedBoundary else None
+        if p.useSuperAbsorbing:
+            self.wx = boundary_weights(nX, band_width(nX, p.boundaryFactor)).astype(self.rdt)
+            self.wy = boundary_weights(nY, band_width(nY, p.boundaryFactor)).astype(self.rdt)
+        self.Ib = np.sum(self.u ** 2, axis=2)
+        return self
+
+    def step(self):
+        p, u, dz = self.p, self.u, self.dz
+        if p.useSplitStep:
+            u = attenuation_step(u, self.af)
+            u = diffraction_step(u, self.H, self.abl)
+            if p.fluxScheme == "kt":
+                u = flux_kt(u, self.N, dz, p.dT)
+            elif p.useTVD:
+                bt = max(1.0, 2.0 - p.adaptiveFilterStrength * (dz / (p.c0 / p.f0)) * 10)
+                u = flux_rusanov_tvd(u, self.N, dz, p.dT, bt)
+            else:
+                u = flux_rusanov(u, self.N, dz, p.dT)
+            u = diffraction_step(u, self.H, self.abl)
+            u = attenuation_step(u, self.af)
+        else:
+            u = diffraction_step(u, self.H, self.abl)
+            u = flux_rusanov(u, self.N, dz, p.dT)
+            u = attenuation_step(u, self.af)
+        if self.fw is not None:
+            u = freq_weighted_step(u, self.fw)
+        if p.useSuperAbsorbing:
+            u = super_absorbing_step(u, self.wx, self.wy, p.dX, p.dY, p.dT, p.c0,
+                                     p.superAbsorbingStrength)
+        Ia = np.sum(u ** 2, axis=2)
+        self.stats = (np.min(u, axis=2), np.max(u, axis=2), Ia, np.maximum(0, self.Ib - Ia),
+                      u[self.nX // 2, self.nY // 2, :].copy())
+        self.Ib = Ia
+        self.u = u
+        return u

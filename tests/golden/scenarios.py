@@ -60,14 +60,19 @@ def piston_field(nX, nY, nT, dX, dY, dT, f0, p0, radius, focus, ncycles=3, dur=2
     t = t - t.mean()
     X, Y = np.meshgrid(x, y, indexing="ij")
     r2 = X ** 2 + Y ** 2
-    ap = (r2 <= radius ** 2).astype(np.float64)
+    ap = r2 <= radius ** 2
     # converging wave: the rim fires first (pulse centre at t = -delay)
     delay = (r2 / (2.0 * focus * c0)) + X * np.sin(steer) / c0
-    delay = np.where(ap > 0, delay - delay[ap > 0].mean(), 0.0)
+    delay = np.where(ap, delay - delay[ap].mean() if ap.any() else 0.0, 0.0)
     w0 = 2 * np.pi * f0
-    tt = t[None, None, :] + delay[:, :, None]
-    env = np.exp(-(1.05 * tt * w0 / (ncycles * np.pi)) ** (2 * dur))
-    return (ap[:, :, None] * env * np.sin(w0 * tt) * p0).astype(np.float32)
+    out = np.zeros((nX, nY, nT), np.float32)
+    ix, iy = np.nonzero(ap)
+    for s0 in range(0, ix.size, 4096):  # aperture pixels only, in chunks
+        sl = slice(s0, s0 + 4096)
+        tt = t[None, :] + delay[ix[sl], iy[sl]][:, None]
+        env = np.exp(-(1.05 * tt * w0 / (ncycles * np.pi)) ** (2 * dur))
+        out[ix[sl], iy[sl], :] = (env * np.sin(w0 * tt) * p0).astype(np.float32)
+    return out
 
 
 def _screens(nX, nY, seed, zs, with_amp):

@@ -156,3 +156,16 @@ def test_stability_violation_raises():
     p = O.OracleParams(**kw)
     with pytest.raises(O.StabilityError):
         O.solve(u0 * 100.0, p, "fp32")
+
+
+def test_march_runner_matches_solve():
+    """The timing runner steps exactly like solve() (no screens/sources)."""
+    for name in ["strang_kt_fw_sa", "lie_water_quadratic", "strang_tvd_wendland"]:
+        u0, kw, ex = S.build_solve_inputs(name)
+        p = O.OracleParams(**kw)
+        ref = O.solve(u0, p, "fp32")
+        m = O.OracleMarch(u0, p, "fp32").build()
+        for _ in range(len(ref[5])):
+            m.step()
+        assert rel(m.u, ref[0]) < 1e-12
+        assert rel(m.stats[1], ref[2][:, :, -1]) < 1e-6  # solve() stores float32
