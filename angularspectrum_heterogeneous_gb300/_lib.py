@@ -24,7 +24,7 @@ EXPORTED = [
     "asg_plan_create", "asg_plan_destroy", "asg_set_step_operators", "asg_add_screen",
     "asg_add_source", "asg_run", "asg_get_outputs", "asg_last_run_ms", "asg_apply_operator",
     "asg_flux_columns", "asg_last_error", "asg_version", "asg_set_profiling",
-    "asg_kernel_stats",
+    "asg_kernel_stats", "asg_flux_columns_device",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -98,6 +98,9 @@ def load(require_device: bool = True):
     lib.asg_apply_operator.argtypes = [P, C.c_int, F, C.c_int, _DP]
     lib.asg_flux_columns.argtypes = [F, F, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                      C.c_double, C.c_double, C.c_double, C.c_int]
+    lib.asg_flux_columns_device.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_double,
+                                            C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_int, P]
     lib.asg_set_profiling.argtypes = [P, C.c_int]
     lib.asg_kernel_stats.argtypes = [P, _DP, C.POINTER(C.c_long), C.c_int]
     lib.asg_last_error.restype = C.c_char_p

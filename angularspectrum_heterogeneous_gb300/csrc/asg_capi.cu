@@ -15,6 +15,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1255,6 +1256,96 @@ extern "C" int asg_flux_columns(const float* in, float* out, int ncols, int nT, 
   cudaFree(tw);
   if (s != ASG_OK) return fail(s, "flux kernel launch failed");
   if (e != cudaSuccess) return fail(ASG_ERR_CUDA, "%s", cudaGetErrorString(e));
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// asg_flux_columns_device: the Burgers column step on the caller's device
+// buffers and stream, allocating nothing.
+//
+// asg_flux_columns allocates and frees four device buffers on every call. Some
+// callers cannot have that: a host framework whose device memory all belongs
+// to its own pool, a real-time loop in which cudaMalloc/cudaFree (which
+// synchronise the device) are not allowed, or code that queues work on a
+// stream it must not stall. They call this entry point instead. Besides its
+// input and output the column kernel touches two small global areas: a status
+// word it reads first (it must be zero, or the kernel returns without work)
+// and a twiddle area it copies into shared memory (unused here, since the
+// columns go in and out as real samples with no transform). Both live in the
+// fixed array below, whose device address is looked up once per device.
+// ---------------------------------------------------------------------------
+static constexpr int FLUX_SCRATCH_MAX_NT = 2048;  // longest column of the kernel
+static constexpr int FLUX_SCRATCH_MAX_DEVICES = 64;
+
+struct FluxScratch {
+  unsigned status;        // must read zero when the kernel starts
+  unsigned pad[63];       // keeps the twiddle area on its own 256-byte line
+  float2 tw[FLUX_SCRATCH_MAX_NT];
+};  // 16,640 bytes in all
+
+static __device__ __align__(256) FluxScratch g_flux_scratch;
+
+static std::mutex g_flux_scratch_mu;
+static FluxScratch* g_flux_scratch_ptr[FLUX_SCRATCH_MAX_DEVICES];
+
+// Address of the scratch on the current device, looked up on the first call
+// made with that device current.
+static int flux_scratch_on_current_device(FluxScratch** out) {
+  int dev = -1;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= FLUX_SCRATCH_MAX_DEVICES)
+    return fail(ASG_ERR_ARG, "device ordinal %d is beyond the %d devices supported", dev,
+                FLUX_SCRATCH_MAX_DEVICES);
+  std::lock_guard<std::mutex> lock(g_flux_scratch_mu);
+  if (!g_flux_scratch_ptr[dev]) {
+    void* ptr = nullptr;
+    CK(cudaGetSymbolAddress(&ptr, g_flux_scratch));
+    g_flux_scratch_ptr[dev] = static_cast<FluxScratch*>(ptr);
+  }
+  *out = g_flux_scratch_ptr[dev];
+  return ASG_OK;
+}
+
+extern "C" int asg_flux_columns_device(const float* d_in, float* d_out, int ncols, int nT,
+                                       int flux, double n_coef, double dz, double dt,
+                                       double beta_tvd, double cfl_target, int max_subcycles,
+                                       void* stream) {
+  g_err.clear();
+  if (!d_in || !d_out || ncols <= 0 || nT < 3) return fail(ASG_ERR_ARG, "bad argument");
+  if (nT > FLUX_SCRATCH_MAX_NT)
+    return fail(ASG_ERR_SHAPE, "nT=%d exceeds the %d samples the fixed scratch holds", nT,
+                FLUX_SCRATCH_MAX_NT);
+  if (flux < ASG_FLUX_RUSANOV || flux > ASG_FLUX_KT_MINMOD)
+    return fail(ASG_ERR_ARG, "unknown flux %d", flux);
+  FluxScratch* scr = nullptr;
+  CKS(flux_scratch_on_current_device(&scr));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CK(cudaMemsetAsync(&scr->status, 0, sizeof(unsigned), st));
+  TParams t;
+  memset(&t, 0, sizeof(t));
+  t.ncols = ncols;
+  t.nT = nT;
+  t.in_real = 1;
+  t.real_in = const_cast<float*>(d_in);
+  t.write_real = 1;
+  t.real_out = d_out;
+  t.tw = scr->tw;
+  t.status = &scr->status;
+  t.op.flux = flux;
+  t.op.dz = (float)dz;
+  t.op.beta_tvd = (float)beta_tvd;
+  t.op.coef_rus = (float)(n_coef * dz / dt);
+  t.op.coef_kt = (float)(n_coef / dt);
+  t.op.n_rus64 = n_coef * dz / dt;
+  t.op.n_kt64 = n_coef / dt;
+  t.op.cfl_target = (float)cfl_target;
+  t.op.max_subcycles = max_subcycles > 0 ? max_subcycles : 1024;
+  GenPlan gp = make_gen_plan(nT);
+  const int s = asg_launch_t(t, false, gp, st);
+  if (s != ASG_OK) {
+    const cudaError_t e = cudaGetLastError();
+    return fail(s, "flux kernel launch failed: %s", cudaGetErrorString(e));
+  }
   return ASG_OK;
 }
 

@@ -167,6 +167,22 @@ int asg_apply_operator(asg_plan* plan, int op, float* field, int screen_index,
 int asg_flux_columns(const float* in, float* out, int ncols, int nT, int flux, double n_coef,
                      double dz, double dt, double beta_tvd, double cfl_target, int max_subcycles);
 
+/* The same Burgers step on DEVICE buffers (ncols x nT floats each, column-major
+ * as above; d_in == d_out is not allowed), queued on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream). No counterpart in the reference: it exists
+ * for callers that must not allocate device memory (memory owned by their own
+ * pool, loops where a synchronising cudaMalloc/cudaFree is not allowed).
+ * It allocates nothing: its scratch (a status word it clears on `stream` before
+ * each launch, and a twiddle area) is a fixed 16,640-byte array in the library,
+ * whose address is looked up on the first call made with each device current,
+ * so make that first call before any stream capture. nT above 2048 is rejected
+ * with ASG_ERR_SHAPE. Returns once the work is queued; the result is ready when
+ * `stream` is. Two calls in flight at once on one device (different streams or
+ * host threads) share the scratch and race: order them on one stream. */
+int asg_flux_columns_device(const float* d_in, float* d_out, int ncols, int nT, int flux,
+                            double n_coef, double dz, double dt, double beta_tvd,
+                            double cfl_target, int max_subcycles, void* stream);
+
 /* Message of the last error on this thread. */
 const char* asg_last_error(void);
 

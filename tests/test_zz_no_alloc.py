@@ -1,0 +1,70 @@
+"""asg_flux_columns_device: the Burgers column step on device buffers with no
+allocation of its own, checked against asg_flux_columns (host buffers, which
+allocates per call) through the C ABI.
+
+Collected last so it also runs after every other GPU test in the session."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import scenarios as S
+from gpu_helpers import rel
+
+pytestmark = pytest.mark.gpu
+
+N_COEF = 3.5 / (2 * 1540.0 ** 3 * 1000.0)
+CASES = [  # (flux, extra keyword arguments)
+    ("RUSANOV", {}),
+    ("RUSANOV_TVD", {"beta_tvd": 1.7}),
+    ("KT", {}),
+    ("KT_MINMOD", {}),
+    ("KT", {"cfl_target": 0.3}),
+]
+
+
+def _columns(ncols, nT):
+    return np.stack([S.seeded_column(nT, s) * a for s, a in
+                     zip(range(ncols), np.linspace(0.3, 6.0, ncols))]).astype(np.float32)
+
+
+def _device_call(lib, d_in, d_out, ncols, nT, flux, dz, dt, beta_tvd=1.0, cfl_target=0.0,
+                 max_subcycles=1024, stream=None):
+    return lib.asg_flux_columns_device(
+        C.c_void_p(d_in.data_ptr()), C.c_void_p(d_out.data_ptr()), ncols, nT, flux, N_COEF, dz,
+        dt, beta_tvd, cfl_target, max_subcycles, C.c_void_p(stream))
+
+
+@pytest.mark.parametrize("nT", [3, 65, 256, 801, 2048])
+def test_device_entry_matches_host_entry_twice(nT):
+    import torch
+    from angularspectrum_heterogeneous_gb300 import _lib
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    lib = _lib.load()
+    ncols = 37
+    cols = _columns(ncols, nT)
+    dz, dt = 4e-4, 1e-8
+    stream = torch.cuda.current_stream()
+    d_in = torch.from_numpy(cols).cuda()
+    for name, extra in CASES:
+        flux = getattr(_lib, "FLUX_" + name)
+        ref = _lib.flux_columns(cols, flux, N_COEF, dz, dt, **extra)
+        for call in range(2):  # two calls in a row reuse the same scratch
+            d_out = torch.full_like(d_in, float("nan"))
+            _lib.check(_device_call(lib, d_in, d_out, ncols, nT, flux, dz, dt,
+                                    stream=stream.cuda_stream, **extra))
+            stream.synchronize()
+            out = d_out.cpu().numpy()
+            assert np.isfinite(out).all(), (name, call)
+            assert rel(out, ref) < 1e-6, (name, extra, call, rel(out, ref))
+    assert torch.equal(d_in.cpu(), torch.from_numpy(cols)), "input buffer was modified"
+
+
+def test_device_entry_rejects_long_columns():
+    import torch
+    from angularspectrum_heterogeneous_gb300 import _lib
+    lib = _lib.load()
+    d = torch.zeros(2 * 4096, device="cuda")
+    code = _device_call(lib, d, d, 2, 4096, _lib.FLUX_KT, 1e-4, 1e-8)
+    assert code == -2  # ASG_ERR_SHAPE
+    assert b"2048" in lib.asg_last_error()
