@@ -30,8 +30,11 @@ ASG_DEFINE_ROOT_UPLOADER(asg_roots_upload_t)
 // ---------------------------------------------------------------------------
 enum TMode : int { TM_PLAIN = 0, TM_FLUX = 1, TM_STATS = 2 };
 
+// Register budget: the KT window of the flux mode needs up to 128 registers
+// (2 blocks per SM); the other modes run 3 blocks per SM from 512 samples up
+// (shared memory allows no more at 1024) and 4 below.
 template <class PL, int MODE>
-__global__ void __launch_bounds__(256) tk_fast(TParams p) {
+__global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4))) tk_fast(TParams p) {
   if (*p.status != 0) return;
   constexpr int C = 8;
   constexpr int M = PL::N;
