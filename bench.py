@@ -204,6 +204,7 @@ def run_reference_arm(args):
 def run_gpu_arm(args):
     import torch
     from angularspectrum_heterogeneous_gb300 import Plan, angular_spectrum_solve
+    from angularspectrum_heterogeneous_gb300.replicas import max_over_ranks
     from angularspectrum_heterogeneous_gb300.solver import initial_step
 
     rank = int(os.environ.get("RANK", "0"))
@@ -228,12 +229,9 @@ def run_gpu_arm(args):
     with Clocks() as clk:
         plan.run(u0, args.steps * dz, dz)
     torch.cuda.synchronize()
-    ms = plan.last_run_ms()
-    t = torch.tensor([ms], device="cuda")
+    ms = max_over_ranks(plan.last_run_ms(), device="cuda")
     if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dist.barrier()
-    ms = float(t.item())
     launches = sum(v[1] for v in plan.kernel_stats().values())
     # per-kernel device times (separate profiled pass of the same K steps)
     plan.set_profiling(True)
