@@ -30,7 +30,11 @@ struct TParams {
   const float2* tw;      // W_nT^k, k < nT
   const float2* twM;     // W_M^k,  k < M (fast kernels)
   const unsigned* status;
+  int cols_per_block;    // fast kernels: 8 or 16 columns per block, 0 = default
 };
+
+int asg_t_default_cols(int nT, int Y, int flux);
+bool asg_t_cols_supported(int nT, int Y, int flux, int cols);
 
 bool asg_t_fast_supported(int nT);
 size_t asg_t_generic_smem(int nT);

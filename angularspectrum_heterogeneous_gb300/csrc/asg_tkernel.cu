@@ -20,28 +20,35 @@ ASG_DEFINE_ROOT_UPLOADER(asg_roots_upload_t)
 
 // ---------------------------------------------------------------------------
 // fast kernel: nT = 2M, M = N1*N2 (register-resident four-step FFT).
-// A block handles 8 columns: 4 consecutive y at x and the same 4 y at x+X/2
-// (warps 0-3 and 4-7).  That pairing lets the kernel apply the first radix-2
-// stage of the x transform on the way out (split_out: planes hold
-// a = (s(x) + s(x+X/2))/2 and b = (s(x) - s(x+X/2)) W_X^x/2 in rows x and x+X/2) and
-// undo it on the way in (split_in: s = a +/- W_X^-x b), so the plane kernels
-// work on X/2-row half-planes (their transforms are normalised by the
-// half-plane size).  MODE selects the column work at compile time.
+// A block of 8 warps handles C columns (C = 8 or 16): CY = C/2 consecutive y
+// at row x and the same CY y at row x+X/2.  That pairing lets the kernel
+// apply the first radix-2 stage of the x transform on the way out
+// (split_out: planes hold a = (s(x) + s(x+X/2))/2 and
+// b = (s(x) - s(x+X/2)) W_X^x/2 in rows x and x+X/2) and undo it on the way in
+// (split_in: s = a +/- W_X^-x b), so the plane kernels work on X/2-row
+// half-planes (their transforms are normalised by the half-plane size).
+// Warp w owns columns w, w+8, ... (CPW = C/8 of them); with C = 16 the N1
+// tasks of step B of two columns fill the 32 lanes of a warp, and each
+// frequency plane is read and written in 64-byte runs.  MODE selects the
+// column work at compile time.
 // ---------------------------------------------------------------------------
 enum TMode : int { TM_PLAIN = 0, TM_FLUX = 1, TM_STATS = 2 };
 
 // Register budget: the KT window of the flux mode needs up to 128 registers
-// (2 blocks per SM); the other modes run 3 blocks per SM from 512 samples up
-// (shared memory allows no more at 1024) and 4 below.
-template <class PL, int MODE>
-__global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4))) tk_fast(TParams p) {
+// (2 blocks per SM); the other modes run 3 blocks per SM with 16 columns or
+// from 512 samples up (shared memory allows no more) and 4 otherwise.
+template <class PL, int MODE, int C>
+__global__ void __launch_bounds__(256, (MODE == 1 ? 2 : ((PL::N >= 512 || C == 16) ? 3 : 4)))
+    tk_fast(TParams p) {
   if (*p.status != 0) return;
-  constexpr int C = 8;
+  static_assert(C == 8 || C == 16, "8 or 16 columns per block");
+  constexpr int CPW = C / 8;   // columns per warp
+  constexpr int CY = C / 2;    // consecutive y per row
   constexpr int M = PL::N;
   constexpr int N1 = PL::N1;
   constexpr int N2 = PL::N2;
   constexpr int CH = (2 * M + 31) / 32;
-  // column stride: padded line + 2, so the 8 columns of a tile fall in
+  // column stride: padded line + 2, so the columns of a tile fall in
   // different shared-memory banks in the pair (k, M-k) phases
   constexpr int LS = PL::PADDED + 2;
   const int nT = 2 * M;
@@ -49,28 +56,32 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
   float2* lines = reinterpret_cast<float2*>(smraw);
   float2* stage = lines + C * LS;                       // TM_FLUX only
   float2* twM = stage + (MODE == TM_FLUX ? C * LS : 0);
-  float2* twT = twM + M;
-  __shared__ float red_max[C];
+  const float2* __restrict__ twT = p.tw;                // W_2M^k, k <= M (L1-cached)
+  __shared__ float red_max[8];
 
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int X = p.X, Y = p.Y, X2 = p.X / 2;
+  const int Y = p.Y, X2 = p.X / 2;
   const int ncols = p.ncols;
-  // tile -> (x, y0); columns of warp w: x + (w>=4)*X2, y0 + (w&3)
+  // tile -> (x, y0); column cc: row x + (cc >= CY)*X/2, y = y0 + cc % CY
   const int tile = blockIdx.x;
-  const int xq = tile / (Y / 4), y0 = 4 * (tile - xq * (Y / 4));
+  const int xq = tile / (Y / CY), y0 = CY * (tile - xq * (Y / CY));
   for (int i = tid; i < M; i += nthr) twM[i] = p.twM[i];
-  for (int i = tid; i <= M; i += nthr) twT[i] = p.tw[i];
   const float2 wx = p.twX[xq];  // W_X^x of this tile's column pair
-
-  float2* myline = lines + warp * LS;
-  const int mycol = (xq + (warp >= 4 ? X2 : 0)) * Y + y0 + (warp & 3);
+  auto col_of = [&](int cc) {
+    return (xq + (cc >= CY ? X2 : 0)) * Y + y0 + (cc & (CY - 1));
+  };
 
   // ---------------- phase 1: input ----------------
   if (p.in_real) {
     __syncthreads();
-    const float2* src = reinterpret_cast<const float2*>(p.real_in + (size_t)mycol * nT);
-    for (int j = lane; j < M; j += 32) myline[PL::pos(j)] = src[j];
+#pragma unroll
+    for (int j = 0; j < CPW; ++j) {
+      const int cc = warp + 8 * j;
+      float2* line = lines + cc * LS;
+      const float2* src = reinterpret_cast<const float2*>(p.real_in + (size_t)col_of(cc) * nT);
+      for (int i = lane; i < M; i += 32) line[PL::pos(i)] = src[i];
+    }
     __syncwarp();
   } else {
     __syncthreads();
@@ -79,8 +90,8 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
     const size_t colA = (size_t)xq * Y + y0;        // row x
     const size_t colB = colA + (size_t)X2 * Y;       // row x + X/2
 #pragma unroll 2
-    for (int it = tid; it < npairs * 4; it += nthr) {
-      const int u = it & 3, k = it >> 2;
+    for (int it = tid; it < npairs * CY; it += nthr) {
+      const int u = it & (CY - 1), k = it / CY;
       const int k2 = M - k;
       const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
       const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
@@ -96,12 +107,13 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
         mb = csub(m0, tm);
       }
       float2* la = lines + u * LS;
-      float2* lb = lines + (u + 4) * LS;
+      float2* lb = lines + (u + CY) * LS;
       if (k == 0) {
         // bins 0 and M: imaginary parts dropped (irfft)
         la[PL::pos(0)] = make_float2((xa.x + ma.x) * inv2M, (xa.x - ma.x) * inv2M);
         lb[PL::pos(0)] = make_float2((xb.x + mb.x) * inv2M, (xb.x - mb.x) * inv2M);
       } else {
+        const float2 wk = __ldg(twT + k);
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
           const float2 xk = side ? xb : xa;
@@ -109,7 +121,7 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
           float2* line = side ? lb : la;
           const float2 E = make_float2(0.5f * (xk.x + xm.x), 0.5f * (xk.y - xm.y));
           const float2 D = make_float2(0.5f * (xk.x - xm.x), 0.5f * (xk.y + xm.y));
-          const float2 O = cmulc(D, twT[k]);
+          const float2 O = cmulc(D, wk);
           // Z[k] = E + iO ; Z[M-k] = conj(E) + i conj(O)
           line[PL::pos(sk)] = make_float2((E.x - O.y) * (2.f * inv2M), (E.y + O.x) * (2.f * inv2M));
           line[PL::pos(sk2)] = make_float2((E.x + O.y) * (2.f * inv2M), (-E.y + O.x) * (2.f * inv2M));
@@ -117,24 +129,35 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
       }
     }
     __syncthreads();
-    // inverse four-step on my column: B^-1 then A^-1
-    for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, true>(myline, ka);
+    // inverse four-step on my columns: B^-1 then A^-1
+    for (int i = lane; i < CPW * N1; i += 32) {
+      const int j = i / N1, ka = i - j * N1;
+      stepB_smem<PL, true>(lines + (warp + 8 * j) * LS, ka);
+    }
     __syncwarp();
-    for (int b = lane; b < N2; b += 32) stepA_inv_smem<PL>(myline, b, twM);
+    for (int i = lane; i < CPW * N2; i += 32) {
+      const int j = i / N2, b = i - j * N2;
+      stepA_inv_smem<PL>(lines + (warp + 8 * j) * LS, b, twM);
+    }
     __syncwarp();
   }
 
   // ---------------- phase 2: column work ----------------
   float am = 0.f;
-  {
-    PaddedColumn<N2> col{reinterpret_cast<float*>(myline)};
-    PaddedColumn<N2> stg{reinterpret_cast<float*>(MODE == TM_FLUX ? stage + warp * LS : myline)};
+#pragma unroll
+  for (int j = 0; j < CPW; ++j) {
+    const int cc = warp + 8 * j;
+    float2* line = lines + cc * LS;
+    const int mycol = col_of(cc);
+    PaddedColumn<N2> col{reinterpret_cast<float*>(line)};
+    PaddedColumn<N2> stg{reinterpret_cast<float*>(MODE == TM_FLUX ? stage + cc * LS : line)};
     ColumnOps op = p.op;
     if (MODE != TM_FLUX) op.flux = FLUX_NONE;
-    am = column_phase<CH>(col, stg, mycol, nT, op, MODE == TM_STATS);
+    const float a = column_phase<CH>(col, stg, mycol, nT, op, MODE == TM_STATS);
+    am = (a != a || am != am) ? __uint_as_float(0x7fc00000u) : fmaxf(am, a);
     if (p.write_real) {
       float2* dst = reinterpret_cast<float2*>(p.real_out + (size_t)mycol * nT);
-      for (int j = lane; j < M; j += 32) dst[j] = myline[PL::pos(j)];
+      for (int i = lane; i < M; i += 32) dst[i] = line[PL::pos(i)];
     }
   }
   if (MODE == TM_STATS) {
@@ -143,7 +166,7 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
     if (tid == 0) {
       float m = 0.f;
       bool bad = false;
-      for (int w = 0; w < C; ++w) {
+      for (int w = 0; w < 8; ++w) {
         float v = red_max[w];
         bad |= (v != v);
         m = fmaxf(m, v);
@@ -155,24 +178,31 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
   if (!p.do_r2c) return;
 
   // ---------------- phase 3: forward real FFT ----------------
-  for (int b = lane; b < N2; b += 32) stepA_fwd_smem<PL, false>(myline, b, twM);
+  for (int i = lane; i < CPW * N2; i += 32) {
+    const int j = i / N2, b = i - j * N2;
+    stepA_fwd_smem<PL, false>(lines + (warp + 8 * j) * LS, b, twM);
+  }
   __syncwarp();
-  for (int ka = lane; ka < N1; ka += 32) stepB_smem<PL, false>(myline, ka);
+  for (int i = lane; i < CPW * N1; i += 32) {
+    const int j = i / N1, ka = i - j * N1;
+    stepB_smem<PL, false>(lines + (warp + 8 * j) * LS, ka);
+  }
   __syncthreads();
   {
     const int npairs = M / 2 + 1;
     const size_t colA = (size_t)xq * Y + y0;
     const size_t colB = colA + (size_t)X2 * Y;
 #pragma unroll 2
-    for (int it = tid; it < npairs * 4; it += nthr) {
-      const int u = it & 3, k = it >> 2;
+    for (int it = tid; it < npairs * CY; it += nthr) {
+      const int u = it & (CY - 1), k = it / CY;
       const int k2 = M - k;
       const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
       const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
+      const float2 wk = (k == 0) ? make_float2(1.f, 0.f) : __ldg(twT + k);
       float2 ra[2], rb[2];  // [0]: bin k, [1]: bin M-k, for rows x and x+X/2
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
-        const float2* line = lines + (u + 4 * side) * LS;
+        const float2* line = lines + (u + CY * side) * LS;
         float2 r0, r1;
         if (k == 0) {
           const float2 z = line[PL::pos(0)];
@@ -184,7 +214,7 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : (PL::N >= 512 ? 3 : 4)))
           const float2 E = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
           const float2 D = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
           const float2 O = make_float2(D.y, -D.x);  // -i/2 (zk - conj zm)
-          const float2 WO = cmul(O, twT[k]);
+          const float2 WO = cmul(O, wk);
           r0 = make_float2(E.x + WO.x, E.y + WO.y);
           r1 = make_float2(E.x - WO.x, -(E.y - WO.y));
         }
@@ -309,29 +339,46 @@ __global__ void __launch_bounds__(128) tk_generic(TParams p, GenPlan pl) {
 // ---------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------
-template <int M, int MODE>
+template <int M, int MODE, int C>
 static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   using PL = FastPlan<M>;
-  constexpr int C = 8;
   constexpr int LS = PL::PADDED + 2;
-  const size_t smem = (size_t)((MODE == TM_FLUX ? 2 : 1) * C * LS + M + M + 1) * sizeof(float2);
+  const size_t smem = (size_t)((MODE == TM_FLUX ? 2 : 1) * C * LS + M) * sizeof(float2);
   static bool attr_done = false;
   if (!attr_done) {
-    if (cudaFuncSetAttribute(tk_fast<PL, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(tk_fast<PL, MODE, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return ASG_ERR_CUDA;
     attr_done = true;
   }
-  const int grid = (p.X / 2) * (p.Y / 4);
-  tk_fast<PL, MODE><<<grid, 32 * C, smem, st>>>(p);
+  const int grid = (p.X / 2) * (p.Y / (C / 2));
+  tk_fast<PL, MODE, C><<<grid, 256, smem, st>>>(p);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
+// 16 columns per block exist for the transform-only and statistics modes up
+// to 512-point lines (three blocks of 256 threads still fit an SM).
+bool asg_t_cols_supported(int nT, int Y, int flux, int cols) {
+  if (cols == 8) return Y % 4 == 0;
+  if (cols == 16) return !flux && nT <= 1024 && Y % 8 == 0;
+  return false;
+}
+
+int asg_t_default_cols(int nT, int Y, int flux) {
+  return asg_t_cols_supported(nT, Y, flux, 16) ? 16 : 8;
 }
 
 template <int M>
 static int launch_fast_t(const TParams& p, cudaStream_t st) {
-  if (p.stats) return launch_fast_t_mode<M, TM_STATS>(p, st);
-  if (p.op.flux != FLUX_NONE) return launch_fast_t_mode<M, TM_FLUX>(p, st);
-  return launch_fast_t_mode<M, TM_PLAIN>(p, st);
+  const bool flux = p.op.flux != FLUX_NONE && !p.stats;
+  int c = p.cols_per_block ? p.cols_per_block : asg_t_default_cols(2 * M, p.Y, flux);
+  if (!asg_t_cols_supported(2 * M, p.Y, flux, c)) return ASG_ERR_SHAPE;
+  if (p.stats)
+    return c == 16 ? launch_fast_t_mode<M, TM_STATS, (M <= 512 ? 16 : 8)>(p, st)
+                   : launch_fast_t_mode<M, TM_STATS, 8>(p, st);
+  if (flux) return launch_fast_t_mode<M, TM_FLUX, 8>(p, st);
+  return c == 16 ? launch_fast_t_mode<M, TM_PLAIN, (M <= 512 ? 16 : 8)>(p, st)
+                 : launch_fast_t_mode<M, TM_PLAIN, 8>(p, st);
 }
 
 bool asg_t_fast_supported(int nT) {

@@ -61,10 +61,11 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   constexpr int Y = PY::N, RS = PY::PADDED;
   constexpr int Xs = PX::N;
   constexpr int NW = NT / 32;
-  const int G = p.G;                 // = Xs / R
-  const int Yc = Y / G;              // y-columns per CTA in stage 2
-  const int TS = Yc;                 // row stride of the column tile (complex): lanes run
+  constexpr int G = Xs / R;          // CTAs per cluster (the launcher checks p.G == G)
+  constexpr int Yc = Y / G;          // y-columns per CTA in stage 2
+  constexpr int TS = Yc;             // row stride of the column tile (complex): lanes run
                                      // along c, so the strided x accesses are conflict free
+  static_assert(Xs % R == 0 && Y % G == 0 && Yc % 2 == 0, "tile shape");
   extern __shared__ float4 smraw[];
   float2* buf = reinterpret_cast<float2*>(smraw);       // rows [R][RS] or tile [Xs][TS]
   __shared__ float red[2][NW];
@@ -303,6 +304,7 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
   using PX = FastPlan<Xn>;
   constexpr int R = 16, NT = 256;
   XYParams p = pin;
+  if (p.G != Xn / R) return ASG_ERR_SHAPE;
   const int Yc = Yn / p.G;
   const int nbuf = (R * PY::PADDED > Xn * Yc) ? R * PY::PADDED : Xn * Yc;
   p.l2_buf_elems = nbuf;
