@@ -66,6 +66,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   constexpr int TS = Yc;             // row stride of the column tile (complex): lanes run
                                      // along c, so the strided x accesses are conflict free
   static_assert(Xs % R == 0 && Y % G == 0 && Yc % 2 == 0, "tile shape");
+  constexpr int RPW = R / NW;        // rows per warp in stages 1 and 3
+  static_assert(R % NW == 0, "rows per warp");
   extern __shared__ float4 smraw[];
   float2* buf = reinterpret_cast<float2*>(smraw);       // rows [R][RS] or tile [Xs][TS]
   __shared__ float red[2][NW];
@@ -117,24 +119,35 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     float2* S = scratch0 + (size_t)par * Xs * Y;
     par ^= 1;
     if (issued != q) {
-      for (int r = warp; r < R; r += NW) prefetch_row(q, r);
+#pragma unroll
+      for (int j = 0; j < RPW; ++j) prefetch_row(q, warp + NW * j);
       cp_async_commit();
     }
     cp_async_wait_all();
     __syncthreads();
 
-    // ---- 1. forward y FFT on my rows, rows -> scratch (slot order) ----
-    for (int r = warp; r < R; r += NW) {
-      float2* row = buf + r * RS;
-      for (int b = lane; b < PY::N2; b += 32) stepA_fwd_smem<PY, false>(row, b, tw_y);
-      __syncwarp();
-      for (int ka = lane; ka < PY::N1; ka += 32) stepB_smem<PY, false>(row, ka);
-      __syncwarp();
+    // ---- 1. forward y FFT on my rows (warp w: rows w + NW j, both rows'
+    //      tasks share the warp's lanes), rows -> scratch (slot order) ----
+    for (int i = lane; i < RPW * PY::N2; i += 32) {
+      const int j = i / PY::N2, b = i - j * PY::N2;
+      stepA_fwd_smem<PY, false>(buf + (warp + NW * j) * RS, b, tw_y);
+    }
+    __syncwarp();
+    for (int i = lane; i < RPW * PY::N1; i += 32) {
+      const int j = i / PY::N1, ka = i - j * PY::N1;
+      stepB_smem<PY, false>(buf + (warp + NW * j) * RS, ka);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < RPW; ++j) {
+      const int r = warp + NW * j;
+      const float2* row = buf + r * RS;
       float4* dst = reinterpret_cast<float4*>(S + (size_t)(rank * R + r) * Y);
       for (int s2 = lane; s2 < Y / 2; s2 += 32)
         dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
     }
-    __threadfence();  // scratch writes visible to the other CTAs of the cluster
+    // the cluster barrier's arrive (release) / wait (acquire) pair orders these
+    // global writes before the other CTAs' reads of the scratch
     if (G > 1) cl.sync();
     else __syncthreads();
 
@@ -237,7 +250,6 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
             *reinterpret_cast<const float4*>(buf + x * TS + c2);
       }
     }
-    __threadfence();
     if (G > 1) cl.sync();
     else __syncthreads();
 
@@ -253,22 +265,28 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     const bool pref = qn < nq;
     __syncthreads();
     float2* gbase = sub_base(q) + (size_t)rank * R * Y;
-    for (int r = warp; r < R; r += NW) {
-      float2* row = buf + r * RS;
+    for (int i = lane; i < RPW * PY::N1; i += 32) {
+      const int j = i / PY::N1, ka = i - j * PY::N1;
+      stepB_smem<PY, true>(buf + (warp + NW * j) * RS, ka);
+    }
+    __syncwarp();
+    for (int i = lane; i < RPW * PY::N2; i += 32) {
+      const int j = i / PY::N2, b = i - j * PY::N2;
+      const int r = warp + NW * j;
+      const float2* row = buf + r * RS;
       float2* grow = gbase + (size_t)r * Y;
-      for (int ka = lane; ka < PY::N1; ka += 32) stepB_smem<PY, true>(row, ka);
-      __syncwarp();
-      for (int b = lane; b < PY::N2; b += 32) {
-        float2 v[PY::N1];
-        v[0] = row[PY::pos(b)];
+      float2 v[PY::N1];
+      v[0] = row[PY::pos(b)];
 #pragma unroll
-        for (int ka = 1; ka < PY::N1; ++ka) v[ka] = cmulc(row[PY::pos(b + PY::N2 * ka)], tw_y[b * ka]);
-        dft<PY::N1, true>(v);
+      for (int ka = 1; ka < PY::N1; ++ka) v[ka] = cmulc(row[PY::pos(b + PY::N2 * ka)], tw_y[b * ka]);
+      dft<PY::N1, true>(v);
 #pragma unroll
-        for (int a = 0; a < PY::N1; ++a) grow[b + PY::N2 * a] = v[a];
-      }
-      __syncwarp();
-      if (pref) prefetch_row(qn, r);
+      for (int a = 0; a < PY::N1; ++a) grow[b + PY::N2 * a] = v[a];
+    }
+    __syncwarp();
+    if (pref) {
+#pragma unroll
+      for (int j = 0; j < RPW; ++j) prefetch_row(qn, warp + NW * j);
     }
     if (pref) {
       cp_async_commit();
