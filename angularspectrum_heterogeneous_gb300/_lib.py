@@ -24,7 +24,8 @@ EXPORTED = [
     "asg_plan_create", "asg_plan_destroy", "asg_set_step_operators", "asg_add_screen",
     "asg_add_source", "asg_run", "asg_get_outputs", "asg_last_run_ms", "asg_apply_operator",
     "asg_flux_columns", "asg_last_error", "asg_version", "asg_set_profiling",
-    "asg_kernel_stats", "asg_flux_columns_device",
+    "asg_kernel_stats", "asg_flux_columns_device", "asg_get_tuning", "asg_set_tuning",
+    "asg_autotune",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -56,6 +57,14 @@ class Config(C.Structure):
 
 
 _DP = C.POINTER(C.c_double)
+
+
+class Tuning(C.Structure):
+    _fields_ = [("t_cols_flux", C.c_int), ("t_cols_plain", C.c_int),
+                ("t_cols_stats", C.c_int), ("xy_clusters", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class StepOps(C.Structure):
@@ -101,6 +110,9 @@ def load(require_device: bool = True):
     lib.asg_flux_columns_device.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_double,
                                             C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, P]
+    lib.asg_get_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.asg_set_tuning.argtypes = [P, C.POINTER(Tuning)]
+    lib.asg_autotune.argtypes = [P, F, C.c_double, C.c_int, C.POINTER(Tuning)]
     lib.asg_set_profiling.argtypes = [P, C.c_int]
     lib.asg_kernel_stats.argtypes = [P, _DP, C.POINTER(C.c_long), C.c_int]
     lib.asg_last_error.restype = C.c_char_p

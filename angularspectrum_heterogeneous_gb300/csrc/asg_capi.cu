@@ -183,6 +183,8 @@ struct asg_plan {
   bool split;  // half-plane transforms: the column pass applies the first radix-2 x stage
   bool l2;     // plane kernel with the x exchange through an L2-resident scratch
   int G, nsub;
+  int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
+  int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   float2* l2_scratch = nullptr;
   int* l2_cls_x = nullptr;
   float2* spec2 = nullptr;  // whole-plane output of the epilogue pass
@@ -814,13 +816,23 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.power_acc = p->power_acc;
   x.l2_scratch = p->l2_scratch;
   x.l2_cls_x = p->l2_cls_x;
-  x.l2_max_clusters = L2_MAX_CLUSTERS;
+  x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
+                          ? p->xy_clusters : L2_MAX_CLUSTERS;
   return x;
+}
+
+// which tuning slot a column pass uses: 0 Burgers step, 1 taper only, 2 statistics
+static int t_slot(const TParams& t) {
+  if (t.stats) return 2;
+  return t.op.flux != FLUX_NONE ? 0 : 1;
 }
 
 static int run_t(asg_plan* p, const TParams& t, int kind = ASG_K_OTHER) {
   KScope k(p, kind);
-  return asg_launch_t(t, p->tfast, p->gp_t, p->st);
+  if (!p->tfast) return asg_launch_t(t, false, p->gp_t, p->st);
+  TParams tt = t;
+  tt.cols_per_block = p->t_cols[t_slot(t)];
+  return asg_launch_t(tt, true, p->gp_t, p->st);
 }
 static int run_xy(asg_plan* p, const XYParams& x, int kind = ASG_K_OTHER) {
   KScope k(p, kind);
@@ -1118,6 +1130,97 @@ extern "C" int asg_kernel_stats(asg_plan* p, double* ms, long* launches, int nki
     if (launches) launches[i] = p->launches[i];
   }
   return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch-shape tuning
+// ---------------------------------------------------------------------------
+extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
+  if (!p || !out) return fail(ASG_ERR_ARG, "null argument");
+  const int flux = p->cfg.flux != 0;
+  for (int i = 0; i < 3; ++i) {
+    int c = p->t_cols[i];
+    if (c == 0) c = p->tfast ? asg_t_default_cols(p->T, p->Y, i == 0 ? flux : 0) : 4;
+    (&out->t_cols_flux)[i] = c;
+  }
+  int ncl = p->xy_clusters > 0 ? p->xy_clusters : L2_MAX_CLUSTERS;
+  out->xy_clusters = p->l2 ? ncl : 0;
+  return ASG_OK;
+}
+
+extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
+  g_err.clear();
+  if (!p || !t) return fail(ASG_ERR_ARG, "null argument");
+  const int cols[3] = {t->t_cols_flux, t->t_cols_plain, t->t_cols_stats};
+  for (int i = 0; i < 3; ++i) {
+    if (cols[i] == 0) continue;
+    if (!p->tfast || !asg_t_cols_supported(p->T, p->Y, i == 0, cols[i]))
+      return fail(ASG_ERR_ARG, "%d columns per block not available for nT=%d, nY=%d", cols[i],
+                  p->T, p->Y);
+  }
+  if (t->xy_clusters < 0 || t->xy_clusters > L2_MAX_CLUSTERS)
+    return fail(ASG_ERR_ARG, "xy_clusters %d outside 0..%d", t->xy_clusters, L2_MAX_CLUSTERS);
+  for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
+  p->xy_clusters = t->xy_clusters;
+  return ASG_OK;
+}
+
+// Times each candidate of each knob on `steps` march steps from `field` and
+// keeps the fastest (per-kind device time of the passes the knob drives).
+extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int steps,
+                            asg_tuning* chosen) {
+  g_err.clear();
+  if (!p || !field || !(dz > 0.0) || steps < 1) return fail(ASG_ERR_ARG, "bad argument");
+  if (!p->slot[0].ready) return fail(ASG_ERR_STATE, "operators not set");
+  const bool prof = p->prof;
+  p->prof = true;
+  auto trial = [&](int kind, double* ms) -> int {
+    int n = 0;
+    int s = asg_run(p, field, steps * dz, dz, nullptr, nullptr, &n);
+    if (s != ASG_OK) return s;
+    *ms = p->launches[kind] > 0 ? p->kms[kind] / p->launches[kind] : 0.0;
+    return ASG_OK;
+  };
+  int status = ASG_OK;
+  if (p->tfast) {
+    const int kinds[3] = {ASG_K_T_NONLIN, ASG_K_T_MID, ASG_K_T_END};
+    for (int i = 0; i < 3 && status == ASG_OK; ++i) {
+      if (i == 1 && !p->cfg.split_step) continue;  // no taper-only pass in the Lie march
+      double best = 1e300;
+      int best_c = 0;
+      for (int c : {8, 16}) {
+        if (!asg_t_cols_supported(p->T, p->Y, i == 0, c)) continue;
+        p->t_cols[i] = c;
+        double ms = 0.0;
+        status = trial(kinds[i], &ms);
+        if (status != ASG_OK) break;
+        if (ms < best) {
+          best = ms;
+          best_c = c;
+        }
+      }
+      p->t_cols[i] = best_c;
+    }
+  }
+  if (p->l2 && status == ASG_OK) {
+    double best = 1e300;
+    int best_n = 0;
+    for (int n : {0, 16, 12, 8}) {
+      p->xy_clusters = n;
+      double ms = 0.0;
+      // the plain diffraction pass: B in the Strang march, A in the Lie march
+      status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);
+      if (status != ASG_OK) break;
+      if (ms < best) {
+        best = ms;
+        best_n = n;
+      }
+    }
+    p->xy_clusters = best_n;
+  }
+  p->prof = prof;
+  if (status != ASG_OK) return status;
+  return chosen ? asg_get_tuning(p, chosen) : ASG_OK;
 }
 
 extern "C" int asg_last_run_ms(asg_plan* p, double* ms) {

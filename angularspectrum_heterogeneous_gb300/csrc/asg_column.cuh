@@ -73,6 +73,16 @@ struct PlainColumn {
   ASG_DEV float get(int t) const { return base[t]; }
   ASG_DEV void set(int t, float v) const { base[t] = v; }
 };
+// Skewed copy of a column for the chunked KT step (lane l owns samples
+// 32l .. 32l+31): one pad word per 32 samples puts the 32 lanes' i-th samples
+// in 32 different shared-memory banks.  Holds nT + nT/32 floats.
+struct SkewColumn {
+  float* base;
+  ASG_DEV int idx(int t) const { return t + (t >> 5); }
+  ASG_DEV float get(int t) const { return base[idx(t)]; }
+  ASG_DEV void set(int t, float v) const { base[idx(t)] = v; }
+};
+__host__ __device__ constexpr int skew_floats(int nT) { return nT + nT / 32 + 4; }
 
 // ---------------------------------------------------------------------------
 // flux primitives (float32, same formulas and order as the reference)
@@ -287,9 +297,10 @@ ASG_DEV float column_absmax(const Col& col, int nT) {
 // ---------------------------------------------------------------------------
 // The whole column phase.  CH = ceil(nT/32) samples per lane.
 // ---------------------------------------------------------------------------
-template <int CH, class Col>
+// SKEWED: the KT sub-steps (CH <= 32) run on the per-warp skewed copy `skew`.
+template <int CH, bool SKEWED = false, class Col>
 ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const ColumnOps& op,
-                           bool write_stats) {
+                           bool write_stats, float* skew = nullptr) {
   const int lane = threadIdx.x & 31;
   const unsigned mask = 0xffffffffu;
   // 1) taper
@@ -326,8 +337,32 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
           atomicAdd(op.subcycle_hist + min(nsub, 63), 1u);
       }
       float dzs = op.dz / (float)nsub;
+      if constexpr (CH <= 32 && SKEWED) {
+        {
+          // sub-steps on a bank-conflict-free copy of the column
+          const SkewColumn sk{skew};
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int t = lane + 32 * i;
+            if (t < nT) sk.set(t, col.get(t));
+          }
+          __syncwarp(mask);
+          for (int k = 0; k < nsub; ++k) {
+            if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(sk, nT, ndt, dzs, mask);
+            else kt_column_step_chunk<CH, false>(sk, nT, ndt, dzs, mask);
+          }
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int t = lane + 32 * i;
+            if (t < nT) col.set(t, sk.get(t));
+          }
+          __syncwarp(mask);
+          nsub = 0;
+        }
+      }
       for (int k = 0; k < nsub; ++k) {
-        if constexpr (CH <= 32) {
+        if constexpr (CH <= 32 && SKEWED) {
+        } else if constexpr (CH <= 32) {
           if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(col, nT, ndt, dzs, mask);
           else kt_column_step_chunk<CH, false>(col, nT, ndt, dzs, mask);
         } else {

@@ -52,10 +52,15 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : ((PL::N >= 512 || C == 1
   // different shared-memory banks in the pair (k, M-k) phases
   constexpr int LS = PL::PADDED + 2;
   const int nT = 2 * M;
+  // flux mode: columns up to 1024 samples run the KT sub-steps on one skewed
+  // per-warp copy (SKW floats); longer ones need a stage line per column
+  constexpr bool KT_CHUNK = CH <= 32;
+  constexpr int SKW = skew_floats(2 * M);
+  constexpr int EXTRA = MODE != TM_FLUX ? 0 : (KT_CHUNK ? 8 * SKW / 2 : C * LS);  // float2
   extern __shared__ float4 smraw[];
   float2* lines = reinterpret_cast<float2*>(smraw);
   float2* stage = lines + C * LS;                       // TM_FLUX only
-  float2* twM = stage + (MODE == TM_FLUX ? C * LS : 0);
+  float2* twM = stage + EXTRA;
   const float2* __restrict__ twT = p.tw;                // W_2M^k, k <= M (L1-cached)
   __shared__ float red_max[8];
 
@@ -144,16 +149,20 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? 2 : ((PL::N >= 512 || C == 1
 
   // ---------------- phase 2: column work ----------------
   float am = 0.f;
-#pragma unroll
+#pragma unroll 1
   for (int j = 0; j < CPW; ++j) {
     const int cc = warp + 8 * j;
     float2* line = lines + cc * LS;
     const int mycol = col_of(cc);
     PaddedColumn<N2> col{reinterpret_cast<float*>(line)};
-    PaddedColumn<N2> stg{reinterpret_cast<float*>(MODE == TM_FLUX ? stage + cc * LS : line)};
+    PaddedColumn<N2> stg{
+        reinterpret_cast<float*>((MODE == TM_FLUX && !KT_CHUNK) ? stage + cc * LS : line)};
+    float* skew = (MODE == TM_FLUX && KT_CHUNK) ? reinterpret_cast<float*>(stage) + warp * SKW
+                                                : nullptr;
     ColumnOps op = p.op;
     if (MODE != TM_FLUX) op.flux = FLUX_NONE;
-    const float a = column_phase<CH>(col, stg, mycol, nT, op, MODE == TM_STATS);
+    const float a =
+        column_phase<CH, MODE == TM_FLUX && KT_CHUNK>(col, stg, mycol, nT, op, MODE == TM_STATS, skew);
     am = (a != a || am != am) ? __uint_as_float(0x7fc00000u) : fmaxf(am, a);
     if (p.write_real) {
       float2* dst = reinterpret_cast<float2*>(p.real_out + (size_t)mycol * nT);
@@ -343,7 +352,9 @@ template <int M, int MODE, int C>
 static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   using PL = FastPlan<M>;
   constexpr int LS = PL::PADDED + 2;
-  const size_t smem = (size_t)((MODE == TM_FLUX ? 2 : 1) * C * LS + M) * sizeof(float2);
+  constexpr bool KT_CHUNK = (2 * M + 31) / 32 <= 32;
+  constexpr int EXTRA = MODE != TM_FLUX ? 0 : (KT_CHUNK ? 8 * skew_floats(2 * M) / 2 : C * LS);
+  const size_t smem = (size_t)(C * LS + EXTRA + M) * sizeof(float2);
   static bool attr_done = false;
   if (!attr_done) {
     if (cudaFuncSetAttribute(tk_fast<PL, MODE, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -356,11 +367,13 @@ static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
 }
 
-// 16 columns per block exist for the transform-only and statistics modes up
-// to 512-point lines (three blocks of 256 threads still fit an SM).
+// 16 columns per block exist up to 1024-sample columns (three blocks of 256
+// threads still fit an SM in the transform-only and statistics modes, two in
+// the flux mode).
 bool asg_t_cols_supported(int nT, int Y, int flux, int cols) {
+  (void)flux;
   if (cols == 8) return Y % 4 == 0;
-  if (cols == 16) return !flux && nT <= 1024 && Y % 8 == 0;
+  if (cols == 16) return nT <= 1024 && Y % 8 == 0;
   return false;
 }
 
@@ -376,7 +389,9 @@ static int launch_fast_t(const TParams& p, cudaStream_t st) {
   if (p.stats)
     return c == 16 ? launch_fast_t_mode<M, TM_STATS, (M <= 512 ? 16 : 8)>(p, st)
                    : launch_fast_t_mode<M, TM_STATS, 8>(p, st);
-  if (flux) return launch_fast_t_mode<M, TM_FLUX, 8>(p, st);
+  if (flux)
+    return c == 16 ? launch_fast_t_mode<M, TM_FLUX, (M <= 512 ? 16 : 8)>(p, st)
+                   : launch_fast_t_mode<M, TM_FLUX, 8>(p, st);
   return c == 16 ? launch_fast_t_mode<M, TM_PLAIN, (M <= 512 ? 16 : 8)>(p, st)
                  : launch_fast_t_mode<M, TM_PLAIN, 8>(p, st);
 }

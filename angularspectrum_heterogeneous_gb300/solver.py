@@ -86,6 +86,11 @@ def initial_step(initial_field, params) -> float:
     return max(dz, params.dZmin)
 
 
+# Launch shapes chosen by Plan.autotune, per grid and option set, for this
+# process: later plans with the same key start from them.
+TUNING_CACHE = {}
+
+
 class Plan:
     """One GPU plan: grid, options, operators, screens and sources."""
 
@@ -115,6 +120,33 @@ class Plan:
         self.h = h
         self._keep = []
         self.n_screens = 0
+        self.tuning_key = (self.shape, cfg.flux, cfg.split_step, cfg.freq_weighted,
+                           cfg.super_absorbing, cfg.nonlinear_obliquity, kt_cfl_target > 0)
+        if self.tuning_key in TUNING_CACHE:
+            self.set_tuning(TUNING_CACHE[self.tuning_key])
+
+    def get_tuning(self) -> dict:
+        """Effective launch shapes (columns per block of the three column
+        passes, resident-cluster cap of the plane kernel)."""
+        t = _lib.Tuning()
+        _lib.check(self.lib.asg_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, tuning: dict):
+        t = _lib.Tuning(**{k: int(v) for k, v in tuning.items()})
+        _lib.check(self.lib.asg_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, initial_field, dz: float, steps: int = 2) -> dict:
+        """Time every launch-shape candidate on `steps` march steps from
+        `initial_field`, keep the fastest and remember it for this grid and
+        option set. Overwrites the plan's outputs (run afterwards)."""
+        u0 = np.ascontiguousarray(initial_field, dtype=np.float32)
+        assert u0.shape == self.shape
+        t = _lib.Tuning()
+        _lib.check(self.lib.asg_autotune(self.h, _lib.fptr(u0), float(dz), int(steps),
+                                         C.byref(t)))
+        TUNING_CACHE[self.tuning_key] = t.as_dict()
+        return t.as_dict()
 
     def close(self):
         if getattr(self, "h", None):

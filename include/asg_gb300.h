@@ -155,6 +155,27 @@ int asg_set_profiling(asg_plan* plan, int enable);
  * the last run (counts are kept whether or not profiling is on). */
 int asg_kernel_stats(asg_plan* plan, double* ms, long* launches, int nkinds);
 
+/* Launch shapes of a plan (no counterpart in the reference: its XLA program
+ * has no tunable launch shapes). 0 in a field selects the built-in default. */
+typedef struct {
+  int t_cols_flux;   /* columns per block of the column pass with the Burgers step: 8, 16 */
+  int t_cols_plain;  /* columns per block of the taper-only column pass: 8, 16 */
+  int t_cols_stats;  /* columns per block of the column pass closing a step: 8, 16 */
+  int xy_clusters;   /* cap on resident clusters of the L2-exchange plane kernel: 0..32 */
+} asg_tuning;
+
+/* Effective launch shapes (defaults resolved). */
+int asg_get_tuning(asg_plan* plan, asg_tuning* out);
+
+/* Sets launch shapes; ASG_ERR_ARG for a shape this grid does not support. */
+int asg_set_tuning(asg_plan* plan, const asg_tuning* tuning);
+
+/* Times every candidate of every shape on `steps` march steps from `field`
+ * (host, nX*nY*nT floats) with step dz, keeps the fastest of each and returns
+ * the result in *chosen (may be null). The plan's outputs are overwritten:
+ * tune before the run whose outputs are wanted. */
+int asg_autotune(asg_plan* plan, const float* field, double dz, int steps, asg_tuning* chosen);
+
 /* One step operator on a host field in place (uses the slot-0 operators):
  * op = 1 full diffraction (HH, abl), 2 half diffraction (HH_half, abl_half),
  *      3 full attenuation, 4 half attenuation, 5 frequency-weighted boundary,
