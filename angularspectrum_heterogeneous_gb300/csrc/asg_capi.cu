@@ -187,7 +187,9 @@ struct asg_plan {
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   float2* l2_scratch = nullptr;
   int* l2_cls_x = nullptr;
-  float2* spec2 = nullptr;  // whole-plane output of the epilogue pass
+  float2* spec2 = nullptr;  // whole-plane output of the epilogue pass (DSMEM split path)
+  float2* nyq_tmp = nullptr;  // one plane: epilogue of the Nyquist plane (L2 path)
+  int nyq_plane = -1;         // plane holding bin nT/2, or -1
   GenPlan gp_t, gp_x, gp_y;
   cudaStream_t st;
   cudaEvent_t ev0, ev1;
@@ -304,7 +306,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.map);
     cudaFree(s.val);
   }
-  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->spec, p->spec2, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->spec, p->spec2, p->nyq_tmp, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
@@ -449,7 +451,10 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   // ---- device buffers ----
   const size_t nspec = (size_t)p->F * p->ncols;
   CKS(dalloc(&p->spec, nspec));
-  if (p->split) CKS(dalloc(&p->spec2, nspec));
+  if (p->split && !p->l2) CKS(dalloc(&p->spec2, nspec));
+  for (int q = 0; q < p->F; ++q)
+    if (2 * p->h_f_of_plane[q] == T) p->nyq_plane = q;
+  if (p->l2 && p->nyq_plane >= 0) CKS(dalloc(&p->nyq_tmp, (size_t)X * Y));
   if (p->l2) {
     // scratch for up to L2_MAX_CLUSTERS clusters, two half-planes each
     const int Xs = X / 2;
@@ -818,6 +823,7 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.l2_cls_x = p->l2_cls_x;
   x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
                           ? p->xy_clusters : L2_MAX_CLUSTERS;
+  x.skip_plane = -1;
   return x;
 }
 
@@ -924,6 +930,38 @@ static int closing_stage(asg_plan* p, const float2* table, int epi, int nscr, in
     x.nscreens = nscr;
     x.screens = p->d_screens;
     CKS(run_xy(p, x, kind));
+    t_after.split_in = 0;
+    return ASG_OK;
+  }
+  if (p->l2 && (epi != 0 || nscr > 0)) {
+    // both half-planes of a plane in one cluster, epilogue fused, whole planes
+    // out in place; the Nyquist plane (Re() before the boundary corrections)
+    // goes through the epilogue pass on its own
+    x.epi = epi;
+    x.nscreens = nscr;
+    x.screens = p->d_screens;
+    x.skip_plane = p->nyq_plane;
+    {
+      KScope k(p, kind);
+      CKS(asg_launch_xy_l2_closing(x, p->st));
+    }
+    if (p->nyq_plane >= 0) {
+      const int pl = p->nyq_plane;
+      const size_t pe = (size_t)p->X * p->Y;
+      XYParams e = xyparams(p, nullptr, false);
+      e.epi = epi;
+      e.nscreens = nscr;
+      e.screens = p->d_screens;
+      e.nplanes = 1;
+      e.f_of_plane = p->f_of_plane + pl;
+      if (e.fw_exp) e.fw_exp += pl;
+      if (e.sa_coef) e.sa_coef += pl;
+      if (e.screen_fscale) e.screen_fscale += pl;
+      KScope k(p, ASG_K_OTHER);
+      CKS(asg_launch_epilogue_pass(e, p->spec + pl * pe, p->nyq_tmp, 0, p->st));
+      CK(cudaMemcpyAsync(p->spec + pl * pe, p->nyq_tmp, pe * sizeof(float2),
+                         cudaMemcpyDeviceToDevice, p->st));
+    }
     t_after.split_in = 0;
     return ASG_OK;
   }

@@ -96,12 +96,15 @@ struct XYParams {
   const int* l2_cls_x;     // [nsub][Xs] class of each x slot of the Xs-point FFT
   int l2_buf_elems;        // set by the launcher
   int l2_max_clusters;     // clusters the scratch was sized for
+  int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);
 // L2-exchange plane kernel (asg_xyl2.cu)
 bool asg_xy_l2_supported(int X, int Y, int nsub, int* G_out);
 int asg_launch_xy_l2(const XYParams& p, cudaStream_t st);
+// closing stage with the epilogue fused, whole planes out (same support as above, nsub = 2)
+int asg_launch_xy_l2_closing(const XYParams& p, cudaStream_t st);
 // half-plane kernels (rows x < X/2 and x >= X/2 transformed separately)
 bool asg_xy_split_supported(int X, int Y, int* G_out);
 int asg_launch_epilogue_pass(const XYParams& p, const float2* src, float2* dst, int split,

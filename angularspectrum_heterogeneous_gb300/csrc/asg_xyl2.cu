@@ -297,6 +297,337 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// Closing-stage plane kernel: the attenuation multiplier with the boundary and
+// screen epilogue fused, whole planes out.
+//
+// One cluster owns both half-planes of a plane (the column pass applied the
+// first radix-2 x stage, so rows x < X/2 hold a and rows x >= X/2 hold b):
+//   1. each CTA runs the forward y FFT on its R rows of a and of b and writes
+//      them to the cluster's scratch (rows of a, then rows of b);
+//   2. cluster barrier; per round of YR y-columns, each CTA loads the a and b
+//      tiles, runs the forward x FFT, the multiplier and the inverse x FFT of
+//      both, recombines s(x) = a + W_X^-x b, s(x + X/2) = a - W_X^-x b, and
+//      applies the parts of the epilogue that act along x only: the x factor
+//      of the frequency-weighted damping and the Engquist-Majda x edges.  They
+//      commute with the y transform (coefficients independent of y), so they
+//      run here on y-spectral data with whole x columns at hand;
+//   3. cluster barrier; each CTA reads its whole-plane rows, runs the inverse
+//      y FFT and applies, along the row, the y factor of the damping, the
+//      Engquist-Majda y edges and the phase/amplitude screens, then stores.
+// The order of the epilogue is that of the reference (damping, x edges, then
+// y edges on the x-corrected values, then screens): the y factor of the
+// damping commutes with the x edges.  Re() of bins 0 and nT/2, which the
+// reference takes between the operators, commutes with all of them on bin 0
+// (real coefficients there) and is left to the column pass; the Nyquist plane
+// (p.skip_plane) gets no epilogue here and goes through the epilogue pass.
+// Each CTA reads and writes only its own rows in stages 1 and 3, so one
+// scratch plane per cluster needs no barrier between consecutive planes.
+// (angular_spectrum_solver.py :667-685, :658-664, :144-179, :185-272,
+// :352-390, :1494-1518)
+// ---------------------------------------------------------------------------
+template <class PY, class PX, int R, int NT>
+__global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
+  constexpr int Y = PY::N, RS = PY::PADDED;
+  constexpr int Xs = PX::N, X = 2 * Xs;
+  constexpr int NW = NT / 32;
+  constexpr int G = Xs / R;
+  constexpr int Yc = Y / G;                 // y-columns per CTA in stage 2
+  constexpr int YR = Yc < 16 ? Yc : 16;     // columns per round: tiles [2][Xs][YR]
+  constexpr int NRND = Yc / YR;
+  constexpr int TS = YR;
+  constexpr int RPW = R / NW;
+  static_assert(Xs % R == 0 && Y % G == 0 && Yc % YR == 0 && YR % 2 == 0, "tile shape");
+  static_assert(R % NW == 0 && NT % YR == 0 && X % (NT / YR) == 0, "thread layout");
+  constexpr int CHUNK = X / (NT / YR);      // x per thread in the x-edge walk
+  extern __shared__ float4 smraw[];
+  float2* buf = reinterpret_cast<float2*>(smraw);     // rows [R][RS] or tiles [2][Xs][TS]
+  const int nbuf = p.l2_buf_elems;
+  float2* tw_y = buf + nbuf;
+  float2* tw_x = tw_y + Y;
+  float* gxs = reinterpret_cast<float*>(tw_x + Xs);   // [X] damping x factor, this plane
+  float* gys = gxs + X;                               // [Y] damping y factor, this plane
+  float* wxs = gys + Y;                               // [X] Engquist-Majda weights
+  float* wys = wxs + X;                               // [Y]
+  int* clsy = reinterpret_cast<int*>(wys + Y);
+  int* clsx = clsy + Y;                               // [2][Xs]
+
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (G > 1) ? (int)cl.block_rank() : 0;
+  const int cid = blockIdx.x / G, ncl = gridDim.x / G;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (*((volatile const unsigned*)p.status) != 0u) return;
+
+  for (int i = tid; i < Y; i += NT) {
+    tw_y[i] = p.twY[i];
+    clsy[i] = p.cls_y[i];
+    wys[i] = (p.epi & EPI_SUPERABS) ? p.sa_wy[i] : 0.f;
+  }
+  for (int i = tid; i < Xs; i += NT) tw_x[i] = p.twX[i * 2];  // W_Xs^i
+  for (int i = tid; i < 2 * Xs; i += NT) {
+    clsx[i] = p.l2_cls_x[i];
+    wxs[i] = (p.epi & EPI_SUPERABS) ? p.sa_wx[i] : 0.f;
+  }
+  float2* S = p.l2_scratch + (size_t)cid * X * Y;     // rows of a, then rows of b
+  const bool fw = (p.epi & EPI_FREQW) != 0, sa = (p.epi & EPI_SUPERABS) != 0;
+  const float st = p.sa_strength;
+
+  auto prefetch_row = [&](int plane, int h, int r) {
+    const float2* g = p.spec + ((size_t)plane * X + (size_t)h * Xs + rank * R + r) * Y;
+    float2* d = buf + r * RS;
+    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
+  };
+  int issued = -1;
+
+  for (int plane = cid; plane < p.nplanes; plane += ncl) {
+    const bool epi = plane != p.skip_plane && (p.epi != 0 || p.nscreens > 0);
+    const float cf = sa ? p.sa_coef[plane] : 0.f;   // coeff = -i cf
+    __syncthreads();  // previous plane's users of gxs/gys are done
+    if (fw && epi) {
+      const float e = p.fw_exp[plane];
+      for (int i = tid; i < X; i += NT) gxs[i] = exp2f(e * p.fw_lx[i]);
+      for (int i = tid; i < Y; i += NT) gys[i] = exp2f(e * p.fw_ly[i]);
+    }
+    // ---- 1. forward y FFT of my rows of a and of b -> scratch ----
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      if (issued != plane * 2 + h) {
+#pragma unroll
+        for (int j = 0; j < RPW; ++j) prefetch_row(plane, h, warp + NW * j);
+        cp_async_commit();
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      for (int i = lane; i < RPW * PY::N2; i += 32) {
+        const int j = i / PY::N2, b = i - j * PY::N2;
+        stepA_fwd_smem<PY, false>(buf + (warp + NW * j) * RS, b, tw_y);
+      }
+      __syncwarp();
+      for (int i = lane; i < RPW * PY::N1; i += 32) {
+        const int j = i / PY::N1, ka = i - j * PY::N1;
+        stepB_smem<PY, false>(buf + (warp + NW * j) * RS, ka);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < RPW; ++j) {
+        const int r = warp + NW * j;
+        const float2* row = buf + r * RS;
+        float4* dst = reinterpret_cast<float4*>(S + (size_t)(h * Xs + rank * R + r) * Y);
+        for (int s2 = lane; s2 < Y / 2; s2 += 32)
+          dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
+      }
+      __syncthreads();  // the row buffer is reloaded next
+    }
+    if (G > 1) cl.sync();
+    else __syncthreads();
+
+    // ---- 2. per round: x FFT, multiplier, inverse, recombination, x edges ----
+#pragma unroll 1
+    for (int rnd = 0; rnd < NRND; ++rnd) {
+      const int c0 = rank * Yc + rnd * YR;
+      float2* tile = buf;  // [h][x][c], h-stride Xs*TS
+      for (int i = tid; i < 2 * Xs * YR / 2; i += NT) {
+        const int hx = i / (YR / 2), c2 = 2 * (i - hx * (YR / 2));
+        cp_async16(tile + hx * TS + c2, S + (size_t)hx * Y + c0 + c2);
+      }
+      cp_async_commit();
+      cp_async_wait_all();
+      __syncthreads();
+      for (int it = tid; it < 2 * PX::N2 * YR; it += NT) {
+        const int hb = it / YR, c = it - hb * YR;
+        const int h = hb / PX::N2, b = hb - h * PX::N2;
+        float2* t = tile + h * Xs * TS;
+        float2 v[PX::N1];
+#pragma unroll
+        for (int a = 0; a < PX::N1; ++a) v[a] = t[(b + PX::N2 * a) * TS + c];
+        dft<PX::N1, false>(v);
+        t[b * TS + c] = v[0];
+#pragma unroll
+        for (int ka = 1; ka < PX::N1; ++ka) t[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x[b * ka]);
+      }
+      __syncthreads();
+      for (int it = tid; it < 2 * PX::N1 * YR; it += NT) {
+        const int hk = it / YR, c = it - hk * YR;
+        const int h = hk / PX::N1, ka = hk - h * PX::N1;
+        float2* t = tile + h * Xs * TS;
+        float2 v[PX::N2];
+#pragma unroll
+        for (int b = 0; b < PX::N2; ++b) v[b] = t[(b + PX::N2 * ka) * TS + c];
+        dft<PX::N2, false>(v);
+        const int* cxh = clsx + h * Xs;
+        if (p.table != nullptr) {
+          const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + clsy[c0 + c];
+#pragma unroll
+          for (int kb = 0; kb < PX::N2; ++kb)
+            v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
+        } else {
+          const float nrm = 1.0f / ((float)Xs * (float)Y);
+#pragma unroll
+          for (int kb = 0; kb < PX::N2; ++kb) v[kb] = cscale(v[kb], nrm);
+        }
+        dft<PX::N2, true>(v);
+#pragma unroll
+        for (int b = 0; b < PX::N2; ++b) t[(b + PX::N2 * ka) * TS + c] = v[b];
+      }
+      __syncthreads();
+      for (int it = tid; it < 2 * PX::N2 * YR; it += NT) {
+        const int hb = it / YR, c = it - hb * YR;
+        const int h = hb / PX::N2, b = hb - h * PX::N2;
+        float2* t = tile + h * Xs * TS;
+        float2 v[PX::N1];
+        v[0] = t[b * TS + c];
+#pragma unroll
+        for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(t[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
+        dft<PX::N1, true>(v);
+#pragma unroll
+        for (int a = 0; a < PX::N1; ++a) t[(b + PX::N2 * a) * TS + c] = v[a];
+      }
+      __syncthreads();
+      // recombination (+ damping x factor): tile h=0 <- s(x), h=1 <- s(x + Xs)
+      for (int i = tid; i < Xs * YR; i += NT) {
+        const int x = i / YR, c = i - x * YR;
+        const float2 a = tile[x * TS + c];
+        const float2 wb = cmulc(tile[(Xs + x) * TS + c], __ldg(p.twX + x));
+        float2 s0 = cadd(a, wb), s1 = csub(a, wb);
+        if (fw && epi) {
+          s0 = cscale(s0, gxs[x]);
+          s1 = cscale(s1, gxs[x + Xs]);
+        }
+        tile[x * TS + c] = s0;
+        tile[(Xs + x) * TS + c] = s1;
+      }
+      __syncthreads();
+      if (sa && epi) {
+        // x edges: thread (c, chunk) walks x0 .. x0+CHUNK-1 of column c in place,
+        // with the originals of its two neighbours read before anyone writes
+        const int c = tid % YR, x0 = (tid / YR) * CHUNK;
+        const float2 lo = x0 > 0 ? tile[(x0 - 1) * TS + c] : make_float2(0.f, 0.f);
+        const float2 hi = x0 + CHUNK < X ? tile[(x0 + CHUNK) * TS + c] : make_float2(0.f, 0.f);
+        bool any = false;
+        for (int x = x0; x < x0 + CHUNK; ++x) any |= wxs[x] != 0.f;
+        __syncthreads();
+        if (any) {
+          float2 prev = lo, cur = tile[x0 * TS + c];
+          for (int x = x0; x < x0 + CHUNK; ++x) {
+            const float2 next = x + 1 < x0 + CHUNK ? tile[(x + 1) * TS + c] : hi;
+            const float w = wxs[x];
+            if (w != 0.f) {
+              float2 d;
+              if (x == 0) d = cscale(csub(next, cur), p.sa_invdx);
+              else if (x == X - 1) d = cscale(csub(cur, prev), p.sa_invdx);
+              else d = cscale(csub(next, prev), p.sa_inv2dx);
+              const float2 cd = make_float2(cf * d.y, -cf * d.x);
+              const float2 P = (x < X / 2) ? make_float2(0.5f * (cur.x + cd.x), 0.5f * (cur.y + cd.y))
+                                           : make_float2(0.5f * (cur.x - cd.x), 0.5f * (cur.y - cd.y));
+              tile[x * TS + c] = make_float2(cur.x - st * w * P.x, cur.y - st * w * P.y);
+            }
+            prev = cur;
+            cur = next;
+          }
+        }
+        __syncthreads();
+      }
+      for (int i = tid; i < 2 * Xs * YR / 2; i += NT) {
+        const int hx = i / (YR / 2), c2 = 2 * (i - hx * (YR / 2));
+        *reinterpret_cast<float4*>(S + (size_t)hx * Y + c0 + c2) =
+            *reinterpret_cast<const float4*>(tile + hx * TS + c2);
+      }
+      __syncthreads();  // tile reused by the next round
+    }
+    if (G > 1) cl.sync();
+    else __syncthreads();
+
+    // ---- 3. my whole-plane rows: inverse y FFT, y edges, screens, store ----
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+      for (int j = 0; j < RPW; ++j) {
+        const int r = warp + NW * j;
+        const float4* srcr = reinterpret_cast<const float4*>(S + (size_t)(h * Xs + rank * R + r) * Y);
+        float2* row = buf + r * RS;
+        for (int s2 = lane; s2 < Y / 2; s2 += 32)  // L2 only: other CTAs wrote these
+          *reinterpret_cast<float4*>(row + PY::pos(2 * s2)) = __ldcg(srcr + s2);
+      }
+      __syncwarp();
+      for (int i = lane; i < RPW * PY::N1; i += 32) {
+        const int j = i / PY::N1, ka = i - j * PY::N1;
+        stepB_smem<PY, true>(buf + (warp + NW * j) * RS, ka);
+      }
+      __syncwarp();
+      for (int i = lane; i < RPW * PY::N2; i += 32) {
+        const int j = i / PY::N2, b = i - j * PY::N2;
+        stepA_inv_smem<PY>(buf + (warp + NW * j) * RS, b, tw_y);
+      }
+      __syncwarp();
+#pragma unroll 1
+      for (int j = 0; j < RPW; ++j) {
+        const int r = warp + NW * j;
+        const int x = h * Xs + rank * R + r;
+        const float2* row = buf + r * RS;
+        float2* grow = p.spec + ((size_t)plane * X + x) * Y;
+        if (!epi) {
+          for (int y = lane; y < Y; y += 32) grow[y] = row[PY::pos(y)];
+          continue;
+        }
+        float2 prev_last = make_float2(0.f, 0.f);  // value at y0-1 (damped, not corrected)
+        for (int y0 = 0; y0 < Y; y0 += 32) {
+          const int y = y0 + lane;
+          float2 cur = row[PY::pos(y)];
+          if (fw) cur = cscale(cur, gys[y]);
+          float2 res = cur;
+          if (sa) {
+            float2 left, right;
+            left.x = __shfl_up_sync(0xffffffffu, cur.x, 1);
+            left.y = __shfl_up_sync(0xffffffffu, cur.y, 1);
+            right.x = __shfl_down_sync(0xffffffffu, cur.x, 1);
+            right.y = __shfl_down_sync(0xffffffffu, cur.y, 1);
+            if (lane == 0) left = prev_last;
+            if (lane == 31 && y + 1 < Y) {
+              right = row[PY::pos(y + 1)];
+              if (fw) right = cscale(right, gys[y + 1]);
+            }
+            const float w = wys[y];
+            if (w != 0.f) {
+              float2 d;
+              if (y == 0) d = cscale(csub(right, cur), p.sa_invdy);
+              else if (y == Y - 1) d = cscale(csub(cur, left), p.sa_invdy);
+              else d = cscale(csub(right, left), p.sa_inv2dy);
+              const float2 cd = make_float2(cf * d.y, -cf * d.x);
+              const float2 P = (y < Y / 2) ? make_float2(0.5f * (cur.x + cd.x), 0.5f * (cur.y + cd.y))
+                                           : make_float2(0.5f * (cur.x - cd.x), 0.5f * (cur.y - cd.y));
+              res = make_float2(cur.x - st * w * P.x, cur.y - st * w * P.y);
+            }
+            prev_last.x = __shfl_sync(0xffffffffu, cur.x, 31);
+            prev_last.y = __shfl_sync(0xffffffffu, cur.y, 31);
+          }
+          for (int k = 0; k < p.nscreens; ++k) {
+            const float fs = p.screen_fscale[plane];
+            const ScreenDev sc = p.screens[k];
+            const size_t g = (size_t)x * Y + y;
+            float sn, cs;
+            sincosf(sc.phase[g] * fs, &sn, &cs);
+            res = cmul(res, make_float2(cs, -sn));
+            if (sc.amp != nullptr) {
+              const float a = fminf(fmaxf(sc.amp[g], 1e-6f), 1.0f);
+              res = cscale(res, exp2f(fs * log2f(a)));
+            }
+          }
+          grow[y] = res;
+        }
+      }
+      __syncwarp();
+    }
+    // rows of a of my next plane, while the other warps finish
+    if (plane + ncl < p.nplanes) {
+#pragma unroll
+      for (int j = 0; j < RPW; ++j) prefetch_row(plane + ncl, 0, warp + NW * j);
+      cp_async_commit();
+      issued = (plane + ncl) * 2;
+    }
+  }
+  cp_async_wait_all();
+}
+
+// ---------------------------------------------------------------------------
 bool asg_xy_l2_supported(int X, int Y, int nsub, int* G_out) {
   if (X % nsub) return false;
   const int Xs = X / nsub;
@@ -367,6 +698,62 @@ int asg_launch_xy_l2(const XYParams& p, cudaStream_t st) {
     case 256: return launch_l2<256, 128>(p, st);
     case 384: return launch_l2<384, 192>(p, st);
     case 512: return launch_l2<512, 256>(p, st);
+    default: return ASG_ERR_SHAPE;
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <int Yn, int Xn>
+static int launch_l2c(const XYParams& pin, cudaStream_t st) {
+  using PY = FastPlan<Yn>;
+  using PX = FastPlan<Xn>;
+  constexpr int R = 16, NT = 256;
+  constexpr int G = Xn / R, Yc = Yn / G, YR = Yc < 16 ? Yc : 16;
+  XYParams p = pin;
+  if (p.G != G || p.nsub != 2) return ASG_ERR_SHAPE;
+  const int nbuf = (R * PY::PADDED > 2 * Xn * YR) ? R * PY::PADDED : 2 * Xn * YR;
+  p.l2_buf_elems = nbuf;
+  const size_t smem = (size_t)(nbuf + Yn + Xn) * sizeof(float2) +
+                      (size_t)(2 * (2 * Xn) + 2 * Yn) * sizeof(float) +
+                      (size_t)(Yn + 2 * Xn) * sizeof(int);
+  auto kern = xy_l2c<PY, PX, R, NT>;
+  static int max_clusters = -1;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (max_clusters < 0) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return ASG_ERR_CUDA;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cfg.gridDim = dim3(G * 1024, 1, 1);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) n = 1;
+    max_clusters = n;
+  }
+  int ncl = max_clusters < p.nplanes ? max_clusters : p.nplanes;
+  if (ncl > p.l2_max_clusters) ncl = p.l2_max_clusters;
+  cfg.gridDim = dim3(G * ncl, 1, 1);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
+  return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
+int asg_launch_xy_l2_closing(const XYParams& p, cudaStream_t st) {
+  const int Xs = p.X / p.nsub;
+  switch (p.Y) {
+    case 128: return Xs == 32 ? launch_l2c<128, 32>(p, st) : launch_l2c<128, 64>(p, st);
+    case 192: return launch_l2c<192, 96>(p, st);
+    case 256: return launch_l2c<256, 128>(p, st);
+    case 384: return launch_l2c<384, 192>(p, st);
+    case 512: return launch_l2c<512, 256>(p, st);
     default: return ASG_ERR_SHAPE;
   }
 }

@@ -164,6 +164,13 @@ FAST_CASES = {
     "lie_screens_sources_split": ((64, 128, 128), dict(useSplitStep=False, alpha0=-1.0), 2e6, 8,
                                   dict(zs=[3.0e-4, 7.5e-4, 1.1e-3], amp=[False, True, True]),
                                   dict(zs=[1.0e-4, 5.0e-4, 1.6e-3])),
+    # closing stage with the fused epilogue (both half-planes per cluster): KT,
+    # freq-weighted + super-absorbing, screens and sources, clusters of 4
+    "kt_fw_sa_screens_fused_128": ((128, 128, 256), dict(fluxScheme="kt",
+                                                         useFreqWeightedBoundary=True,
+                                                         useSuperAbsorbing=True), 4e6, 6,
+                                   dict(zs=[3.0e-4, 9.0e-4], amp=[False, True]),
+                                   dict(zs=[5.0e-4, 1.2e-3])),
     # configs[0]-like grid at full size (128^2 x 256) for a few steps
     "c1_grid_tvd_wendland": ((128, 128, 256), dict(fluxScheme="rusanov", boundaryProfile="wendland",
                                                    dX=3.08e-4, dY=3.08e-4, f0=1e6), 4e5, 6),
