@@ -185,6 +185,7 @@ struct asg_plan {
   int G, nsub;
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
+  int xy_clusters_c = 0;      // the same for the closing-stage kernel
   float2* l2_scratch = nullptr;
   int* l2_cls_x = nullptr;
   float2* spec2 = nullptr;  // whole-plane output of the epilogue pass (DSMEM split path)
@@ -941,6 +942,8 @@ static int closing_stage(asg_plan* p, const float2* table, int epi, int nscr, in
     x.nscreens = nscr;
     x.screens = p->d_screens;
     x.skip_plane = p->nyq_plane;
+    x.l2_max_clusters = (p->xy_clusters_c > 0 && p->xy_clusters_c < L2_MAX_CLUSTERS)
+                            ? p->xy_clusters_c : L2_MAX_CLUSTERS;
     {
       KScope k(p, kind);
       CKS(asg_launch_xy_l2_closing(x, p->st));
@@ -1183,6 +1186,8 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   }
   int ncl = p->xy_clusters > 0 ? p->xy_clusters : L2_MAX_CLUSTERS;
   out->xy_clusters = p->l2 ? ncl : 0;
+  ncl = p->xy_clusters_c > 0 ? p->xy_clusters_c : L2_MAX_CLUSTERS;
+  out->xy_clusters_closing = p->l2 ? ncl : 0;
   return ASG_OK;
 }
 
@@ -1196,10 +1201,13 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
       return fail(ASG_ERR_ARG, "%d columns per block not available for nT=%d, nY=%d", cols[i],
                   p->T, p->Y);
   }
-  if (t->xy_clusters < 0 || t->xy_clusters > L2_MAX_CLUSTERS)
-    return fail(ASG_ERR_ARG, "xy_clusters %d outside 0..%d", t->xy_clusters, L2_MAX_CLUSTERS);
+  if (t->xy_clusters < 0 || t->xy_clusters > L2_MAX_CLUSTERS ||
+      t->xy_clusters_closing < 0 || t->xy_clusters_closing > L2_MAX_CLUSTERS)
+    return fail(ASG_ERR_ARG, "cluster caps %d, %d outside 0..%d", t->xy_clusters,
+                t->xy_clusters_closing, L2_MAX_CLUSTERS);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
+  p->xy_clusters_c = t->xy_clusters_closing;
   return ASG_OK;
 }
 
@@ -1255,6 +1263,22 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
       }
     }
     p->xy_clusters = best_n;
+  }
+  // the closing-stage kernel runs when the step has a boundary epilogue
+  if (p->l2 && (p->cfg.freq_weighted || p->cfg.super_absorbing) && status == ASG_OK) {
+    double best = 1e300;
+    int best_n = 0;
+    for (int n : {0, 16, 12, 8}) {
+      p->xy_clusters_c = n;
+      double ms = 0.0;
+      status = trial(ASG_K_XY_C, &ms);
+      if (status != ASG_OK) break;
+      if (ms < best) {
+        best = ms;
+        best_n = n;
+      }
+    }
+    p->xy_clusters_c = best_n;
   }
   p->prof = prof;
   if (status != ASG_OK) return status;

@@ -11,8 +11,8 @@
 //      never leave registers), and writes the columns back;
 //   3. cluster barrier; each CTA reads its rows back, runs the inverse y FFT
 //      and stores the rows to HBM.
-// The scratch is double-buffered between consecutive planes, so a cluster
-// needs only the two barriers per plane.  Shared memory holds either R rows
+// One scratch half-plane per cluster suffices with two barriers per plane:
+// stages 1 and 3 of a CTA touch only its own rows.  Shared memory holds either R rows
 // or Xs x Yc columns, both about 64 KB for 512 x 512 planes split in halves,
 // so two CTAs share an SM.
 //
@@ -107,7 +107,6 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
   };
   int issued = -1;
-  int par = 0;
 
   for (int q = cid; q < nq; q += ncl) {
     const int plane = q / nsub, h = q - (q / nsub) * nsub;
@@ -116,8 +115,10 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int i = tid; i < R * Y / 2; i += NT) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       continue;
     }
-    float2* S = scratch0 + (size_t)par * Xs * Y;
-    par ^= 1;
+    // one scratch half-plane per cluster: in stages 1 and 3 each CTA touches
+    // only its own rows, and the cluster barriers order stage 2's accesses to
+    // all rows after every CTA's stage 3 of the previous plane
+    float2* S = scratch0;
     if (issued != q) {
 #pragma unroll
       for (int j = 0; j < RPW; ++j) prefetch_row(q, warp + NW * j);
@@ -387,7 +388,9 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
       for (int i = tid; i < X; i += NT) gxs[i] = exp2f(e * p.fw_lx[i]);
       for (int i = tid; i < Y; i += NT) gys[i] = exp2f(e * p.fw_ly[i]);
     }
-    // ---- 1. forward y FFT of my rows of a and of b -> scratch ----
+    // ---- 1. forward y FFT of my rows of a and of b -> scratch; each warp
+    //      loads, transforms and stores only its own rows, so it issues the
+    //      loads of its rows of b as soon as its rows of a are stored ----
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
       if (issued != plane * 2 + h) {
@@ -396,7 +399,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         cp_async_commit();
       }
       cp_async_wait_all();
-      __syncthreads();
+      __syncwarp();
       for (int i = lane; i < RPW * PY::N2; i += 32) {
         const int j = i / PY::N2, b = i - j * PY::N2;
         stepA_fwd_smem<PY, false>(buf + (warp + NW * j) * RS, b, tw_y);
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         for (int s2 = lane; s2 < Y / 2; s2 += 32)
           dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
       }
-      __syncthreads();  // the row buffer is reloaded next
+      __syncwarp();  // my rows are reloaded next
     }
     if (G > 1) cl.sync();
     else __syncthreads();

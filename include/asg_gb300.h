@@ -162,6 +162,7 @@ typedef struct {
   int t_cols_plain;  /* columns per block of the taper-only column pass: 8, 16 */
   int t_cols_stats;  /* columns per block of the column pass closing a step: 8, 16 */
   int xy_clusters;   /* cap on resident clusters of the L2-exchange plane kernel: 0..32 */
+  int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..32 */
 } asg_tuning;
 
 /* Effective launch shapes (defaults resolved). */

@@ -36,8 +36,10 @@ def test_every_shape_gives_the_same_march(shape, flux):
         plan.set_operators(0, dz)
         ref = _run(plan, u0, dz)
         default = plan.get_tuning()
-        shapes = [dict(t_cols_flux=8, t_cols_plain=8, t_cols_stats=8, xy_clusters=0),
-                  dict(t_cols_flux=16, t_cols_plain=16, t_cols_stats=16, xy_clusters=3)]
+        shapes = [dict(t_cols_flux=8, t_cols_plain=8, t_cols_stats=8, xy_clusters=0,
+                       xy_clusters_closing=2),
+                  dict(t_cols_flux=16, t_cols_plain=16, t_cols_stats=16, xy_clusters=3,
+                       xy_clusters_closing=0)]
         for tun in shapes:
             plan.set_tuning(tun)
             got = plan.get_tuning()
@@ -46,7 +48,8 @@ def test_every_shape_gives_the_same_march(shape, flux):
             out = _run(plan, u0, dz)
             for k, a, b in zip(KEYS, ref, out):
                 assert np.array_equal(a, b), (tun, k)
-        plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0))
+        plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
+                             xy_clusters_closing=0))
         assert plan.get_tuning() == default
     finally:
         plan.close()
@@ -81,7 +84,7 @@ def test_autotune_picks_a_supported_shape_and_keeps_the_result():
         ref = _run(plan, u0, dz)
         chosen = plan.autotune(u0, dz, steps=2)
         assert chosen["t_cols_flux"] in (8, 16) and chosen["t_cols_plain"] in (8, 16)
-        assert 0 <= chosen["xy_clusters"] <= 32
+        assert 0 <= chosen["xy_clusters"] <= 32 and 0 <= chosen["xy_clusters_closing"] <= 32
         assert solver.TUNING_CACHE[plan.tuning_key] == chosen
         out = _run(plan, u0, dz)
         for k, a, b in zip(KEYS, ref, out):
