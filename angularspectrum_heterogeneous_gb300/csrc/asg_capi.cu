@@ -186,6 +186,12 @@ struct asg_plan {
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
+  // CUDA graph of a regular march step (slot 0, no screen, source, callback,
+  // profiling or output write); rebuilt when `gen` moves on
+  bool use_graphs = true;
+  cudaGraphExec_t step_graph = nullptr;
+  long gen = 0, graph_gen = -1;
+  long graph_launches[ASG_NKINDS] = {};
   float2* l2_scratch = nullptr;
   int* l2_cls_x = nullptr;
   float2* spec2 = nullptr;  // whole-plane output of the epilogue pass (DSMEM split path)
@@ -307,6 +313,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.map);
     cudaFree(s.val);
   }
+  if (p->step_graph) cudaGraphExecDestroy(p->step_graph);
   void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->spec, p->spec2, p->nyq_tmp, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
@@ -594,6 +601,7 @@ extern "C" int asg_set_step_operators(asg_plan* p, int slot, const asg_step_oper
   if (!o->kx || !o->ky || !o->kt || !o->alpha || !o->alpha_star || !o->abl_x || !o->abl_y ||
       !o->abl_t)
     return fail(ASG_ERR_ARG, "missing operator vector");
+  p->gen++;  // tables (and possibly their addresses) change
   const int X = p->X, Y = p->Y, T = p->T, F = p->F;
   Slot& s = p->slot[slot];
   s.dz = o->dz;
@@ -893,6 +901,7 @@ static int nonlinear_stage(asg_plan* p, double dz, double beta_tvd, const float*
 
 static int ensure_outputs(asg_plan* p, int cap) {
   if (p->o_cap >= cap) return ASG_OK;
+  p->gen++;  // the step graph holds the old output pointers
   free_outputs(p);
   const size_t n = (size_t)cap * p->ncols;
   CKS(dalloc(&p->o_pnp, n));
@@ -1024,6 +1033,54 @@ static int march_step(asg_plan* p, const Slot& s, double dzs, double btvd, int n
   return asg_launch_advance(p->d_step, p->d_max_cur, p->d_max_next, p->st);
 }
 
+// A regular step replays the captured graph of one march step.  The first
+// regular step of a run without a valid graph runs eagerly (one-time launcher
+// set-up such as shared-memory attributes happens outside any capture), the
+// next one is captured and instantiated.  Kernels take the step index and the
+// stability maxima from device memory, so every regular step is the same
+// sequence of launches with the same arguments.
+static int regular_step(asg_plan* p, const Slot& s, double dzs, double btvd, bool& seen) {
+  if (p->step_graph && p->graph_gen == p->gen) {
+    CK(cudaGraphLaunch(p->step_graph, p->st));
+    for (int i = 0; i < ASG_NKINDS; ++i) p->launches[i] += p->graph_launches[i];
+    return ASG_OK;
+  }
+  if (!seen) {
+    seen = true;
+    return march_step(p, s, dzs, btvd, 0, 0, false, false);
+  }
+  if (p->step_graph) {
+    cudaGraphExecDestroy(p->step_graph);
+    p->step_graph = nullptr;
+  }
+  long before[ASG_NKINDS];
+  for (int i = 0; i < ASG_NKINDS; ++i) before[i] = p->launches[i];
+  CK(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal));
+  const int st = march_step(p, s, dzs, btvd, 0, 0, false, false);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(p->st, &g);
+  if (st != ASG_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (st != ASG_OK) return st;
+    return fail(ASG_ERR_CUDA, "step capture failed: %s", cudaGetErrorString(e));
+  }
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e2 = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e2 != cudaSuccess) return fail(ASG_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e2));
+  p->step_graph = ex;
+  p->graph_gen = p->gen;
+  for (int i = 0; i < ASG_NKINDS; ++i) p->graph_launches[i] = p->launches[i] - before[i];
+  CK(cudaGraphLaunch(ex, p->st));
+  return ASG_OK;
+}
+
+extern "C" int asg_set_graphs(asg_plan* p, int enable) {
+  if (!p) return fail(ASG_ERR_ARG, "null plan");
+  p->use_graphs = enable != 0;
+  return ASG_OK;
+}
+
 extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double dz,
                        asg_step_cb cb, void* user, int* n_steps_out) {
   g_err.clear();
@@ -1077,6 +1134,7 @@ extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double 
   }
   p->ev_kind.clear();
   CK(cudaEventRecord(p->ev0, p->st));
+  bool regular_seen = false;
   double zcum = 0.0;  // np.cumsum(zvec): plain sequential sum (:1562)
   PySum zsum;
   std::vector<ScreenDev> scr;
@@ -1105,7 +1163,10 @@ extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double 
     const bool last = (k + 1 == steps.size());
     const double norm_step = dzs / (p->cfg.c0 / p->cfg.f0);
     const double btvd = fmax(1.0, 2.0 - p->cfg.adaptive_filter_strength * norm_step * 10);
-    CKS(march_step(p, *s, dzs, btvd, (int)scr.size(), (int)src.size(), last, cb != nullptr));
+    const bool regular = p->use_graphs && !partial && scr.empty() && src.empty() && !last &&
+                         cb == nullptr && !p->prof;
+    if (regular) CKS(regular_step(p, *s, dzs, btvd, regular_seen));
+    else CKS(march_step(p, *s, dzs, btvd, (int)scr.size(), (int)src.size(), last, cb != nullptr));
     zcum += dzs;
     zsum.add(dzs);
     p->zaxis.push_back(zcum);
@@ -1208,6 +1269,7 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
+  p->gen++;
   return ASG_OK;
 }
 
@@ -1281,6 +1343,7 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
     p->xy_clusters_c = best_n;
   }
   p->prof = prof;
+  p->gen++;
   if (status != ASG_OK) return status;
   return chosen ? asg_get_tuning(p, chosen) : ASG_OK;
 }

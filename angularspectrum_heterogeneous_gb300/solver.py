@@ -225,6 +225,10 @@ class Plan:
         _lib.check(self.lib.asg_last_run_ms(self.h, C.byref(v)))
         return v.value
 
+    def set_graphs(self, enable: bool):
+        """Replay regular march steps from one captured CUDA graph (default on)."""
+        _lib.check(self.lib.asg_set_graphs(self.h, int(enable)))
+
     def set_profiling(self, enable: bool):
         _lib.check(self.lib.asg_set_profiling(self.h, int(enable)))
 

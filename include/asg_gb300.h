@@ -155,6 +155,12 @@ int asg_set_profiling(asg_plan* plan, int enable);
  * the last run (counts are kept whether or not profiling is on). */
 int asg_kernel_stats(asg_plan* plan, double* ms, long* launches, int nkinds);
 
+/* Regular march steps (full step, no screen or source crossing, no callback,
+ * profiling off, not the last) replay one captured CUDA graph of the step's
+ * launches; enable = 0 launches every step eagerly.  On by default.  No
+ * counterpart in the reference. */
+int asg_set_graphs(asg_plan* plan, int enable);
+
 /* Launch shapes of a plan (no counterpart in the reference: its XLA program
  * has no tunable launch shapes). 0 in a field selects the built-in default. */
 typedef struct {

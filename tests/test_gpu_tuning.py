@@ -99,3 +99,29 @@ def test_autotune_picks_a_supported_shape_and_keeps_the_result():
             assert got[k] == chosen[k]
     finally:
         plan2.close()
+
+
+@pytest.mark.parametrize("shape,flux", [((64, 128, 256), "kt"), ((16, 14, 64), "rusanov")])
+def test_graph_replay_matches_eager_steps(shape, flux):
+    """Regular steps replayed from the captured step graph give the eager march
+    bit for bit, and a second run reuses the graph."""
+    from angularspectrum_heterogeneous_gb300 import Plan
+    from angularspectrum_heterogeneous_gb300.solver import initial_step
+    params, u0 = _case(shape, flux)
+    dz = initial_step(u0, params)
+    plan = Plan(shape, params)
+    try:
+        plan.set_operators(0, dz)
+        plan.set_graphs(False)
+        eager = _run(plan, u0, dz, steps=7)
+        plan.set_graphs(True)
+        for _ in range(2):
+            out = _run(plan, u0, dz, steps=7)
+            for k, a, b in zip(KEYS, eager, out):
+                assert np.array_equal(a, b), k
+        launches = sum(v[1] for v in plan.kernel_stats().values())
+        plan.set_graphs(False)
+        _run(plan, u0, dz, steps=7)
+        assert launches == sum(v[1] for v in plan.kernel_stats().values())
+    finally:
+        plan.close()
