@@ -2,11 +2,12 @@
 
     from angularspectrum_heterogeneous_gb300 import SolverParams, angular_spectrum_solve
 """
-from .solver import (ASGError, Plan, SolverParams, StabilityError,  # noqa: F401
-                     angular_spectrum_solve)
+from .solver import (ASGError, Batch, Plan, SolverParams, StabilityError,  # noqa: F401
+                     angular_spectrum_solve, solve_batch)
 from .sources import (generate_phase_screen, make_bowl_source,  # noqa: F401
                       make_bowl_source_planes, skull_to_phase_screens)
 
-__all__ = ["SolverParams", "angular_spectrum_solve", "Plan", "ASGError", "StabilityError",
+__all__ = ["SolverParams", "angular_spectrum_solve", "solve_batch", "Plan", "Batch", "ASGError",
+           "StabilityError",
            "make_bowl_source", "make_bowl_source_planes", "generate_phase_screen",
            "skull_to_phase_screens"]

@@ -25,7 +25,8 @@ EXPORTED = [
     "asg_add_source", "asg_run", "asg_get_outputs", "asg_last_run_ms", "asg_apply_operator",
     "asg_flux_columns", "asg_last_error", "asg_version", "asg_set_profiling",
     "asg_kernel_stats", "asg_flux_columns_device", "asg_get_tuning", "asg_set_tuning",
-    "asg_autotune", "asg_set_graphs",
+    "asg_autotune", "asg_set_graphs", "asg_batch_create", "asg_batch_destroy",
+    "asg_batch_set_graphs", "asg_batch_run", "asg_batch_last_run_ms",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -115,6 +116,11 @@ def load(require_device: bool = True):
     lib.asg_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_autotune.argtypes = [P, F, C.c_double, C.c_int, C.POINTER(Tuning)]
     lib.asg_set_graphs.argtypes = [P, C.c_int]
+    lib.asg_batch_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
+    lib.asg_batch_destroy.argtypes = [P]
+    lib.asg_batch_set_graphs.argtypes = [P, C.c_int]
+    lib.asg_batch_run.argtypes = [P, C.POINTER(F), _DP, _DP, C.POINTER(C.c_int)]
+    lib.asg_batch_last_run_ms.argtypes = [P, _DP]
     lib.asg_set_profiling.argtypes = [P, C.c_int]
     lib.asg_kernel_stats.argtypes = [P, _DP, C.POINTER(C.c_long), C.c_int]
     lib.asg_last_error.restype = C.c_char_p

@@ -1081,30 +1081,47 @@ extern "C" int asg_set_graphs(asg_plan* p, int enable) {
   return ASG_OK;
 }
 
-extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double dz,
-                       asg_step_cb cb, void* user, int* n_steps_out) {
-  g_err.clear();
+// State of one run between its steps.
+struct RunState {
+  std::vector<double> steps;    // step sizes
+  std::vector<double> zbefore;  // sum(zvec) before each step
+  double dz = 0.0;
+  double zcum = 0.0;            // np.cumsum(zvec): plain sequential sum (:1562)
+  PySum zsum;
+  bool regular_seen = false;
+};
+
+// Validation, the step sequence, state reset, field upload and the initial
+// column pass (accumulator baselines and the first forward transform).
+static int prepare_run(asg_plan* p, const float* init, double prop_dist, double dz,
+                       RunState& rs) {
   if (!p || !init) return fail(ASG_ERR_ARG, "null argument");
   if (!p->slot[0].ready) return fail(ASG_ERR_STATE, "asg_set_step_operators(slot 0) not called");
   if (fabs(p->slot[0].dz - dz) != 0.0)
     return fail(ASG_ERR_STATE, "slot-0 operators were built for dz=%.17g, run asks %.17g",
                 p->slot[0].dz, dz);
+  rs = RunState();
+  rs.dz = dz;
   // the step sequence, exactly as the reference's while loop forms it
-  std::vector<double> steps;
-  std::vector<double> zbefore;  // sum(zvec) before each step
   {
     PySum zs;
     while (zs.value() < prop_dist - 1e-15) {
       const double rem = prop_dist - zs.value();
       const double d = dz < rem ? dz : rem;
-      zbefore.push_back(zs.value());
-      steps.push_back(d);
+      rs.zbefore.push_back(zs.value());
+      rs.steps.push_back(d);
       zs.add(d);
-      if (steps.size() > 100000000) return fail(ASG_ERR_ARG, "too many steps");
+      if (rs.steps.size() > 100000000) return fail(ASG_ERR_ARG, "too many steps");
     }
   }
   const int cap = (int)ceil(prop_dist / dz) + 100;
-  if ((int)steps.size() > cap) return fail(ASG_ERR_ARG, "step count exceeds output capacity");
+  if ((int)rs.steps.size() > cap) return fail(ASG_ERR_ARG, "step count exceeds output capacity");
+  for (size_t k = 0; k < rs.steps.size(); ++k) {
+    const double dzs = rs.steps[k];
+    if (fabs(dzs - dz) > 1e-15 && (!p->slot[1].ready || p->slot[1].dz != dzs))
+      return fail(ASG_ERR_STATE, "partial step dz=%.17g needs asg_set_step_operators(slot 1)",
+                  dzs);
+  }
   CKS(ensure_outputs(p, cap));
   // state
   CK(cudaMemsetAsync(p->d_status, 0, sizeof(unsigned), p->st));
@@ -1133,58 +1150,307 @@ extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double 
     p->kms[i] = 0.0;
   }
   p->ev_kind.clear();
-  CK(cudaEventRecord(p->ev0, p->st));
-  bool regular_seen = false;
-  double zcum = 0.0;  // np.cumsum(zvec): plain sequential sum (:1562)
-  PySum zsum;
+  return ASG_OK;
+}
+
+// Whether step k can replay the step graph: a full step with no screen or
+// source crossing, not the last, no callback, profiling off.
+static bool step_is_regular(const asg_plan* p, const RunState& rs, size_t k, bool has_cb) {
+  if (!p->use_graphs || has_cb || p->prof || k + 1 == rs.steps.size()) return false;
+  const double dzs = rs.steps[k], z = rs.zbefore[k];
+  if (fabs(dzs - rs.dz) > 1e-15) return false;
+  for (auto& sc : p->screens)
+    if (z < sc.z && sc.z <= z + dzs) return false;
+  for (auto& so : p->sources)
+    if (z < so.z && so.z <= z + dzs) return false;
+  return true;
+}
+
+static double step_btvd(const asg_plan* p, double dzs) {
+  const double norm_step = dzs / (p->cfg.c0 / p->cfg.f0);
+  return fmax(1.0, 2.0 - p->cfg.adaptive_filter_strength * norm_step * 10);
+}
+
+// Step k launched eagerly (screens and sources crossed in (z, z+dZ] uploaded).
+static int eager_step(asg_plan* p, const RunState& rs, size_t k, bool want_real) {
+  const double dzs = rs.steps[k];
+  const double z = rs.zbefore[k];
+  const bool partial = fabs(dzs - rs.dz) > 1e-15;
+  const Slot* s = partial ? &p->slot[1] : &p->slot[0];
   std::vector<ScreenDev> scr;
+  for (auto& sc : p->screens)
+    if (z < sc.z && sc.z <= z + dzs) scr.push_back(ScreenDev{sc.phase, sc.amp});
   std::vector<SourceEvent> src;
-  for (size_t k = 0; k < steps.size(); ++k) {
-    const double dzs = steps[k];
-    const double z = zbefore[k];
-    const bool partial = fabs(dzs - dz) > 1e-15;
-    const Slot* s = &p->slot[0];
-    if (partial) {
-      if (!p->slot[1].ready || p->slot[1].dz != dzs)
-        return fail(ASG_ERR_STATE, "partial step dz=%.17g needs asg_set_step_operators(slot 1)",
-                    dzs);
-      s = &p->slot[1];
+  for (auto& so : p->sources)
+    if (z < so.z && so.z <= z + dzs) src.push_back(SourceEvent{so.map, so.val});
+  if (scr.size() > 64 || src.size() > 64)
+    return fail(ASG_ERR_ARG, "more than 64 screens or sources in one step");
+  if (!scr.empty()) CKS(h2d(p->d_screens, scr.data(), scr.size(), p->st));
+  if (!src.empty()) CKS(h2d(p->d_src, src.data(), src.size(), p->st));
+  const bool last = (k + 1 == rs.steps.size());
+  return march_step(p, *s, dzs, step_btvd(p, dzs), (int)scr.size(), (int)src.size(), last,
+                    want_real);
+}
+
+static void step_done(asg_plan* p, RunState& rs, size_t k) {
+  rs.zcum += rs.steps[k];
+  rs.zsum.add(rs.steps[k]);
+  p->zaxis.push_back(rs.zcum);
+}
+
+static int finish_run(asg_plan* p, const RunState& rs) {
+  collect_kernel_times(p);
+  p->nsteps = (int)rs.steps.size();
+  return status_to_error(p);
+}
+
+// ---------------------------------------------------------------------------
+// Batched march: independent plans (grids of any size) advanced together.
+// Step k of every plan whose step k is regular is issued as ONE graph launch:
+// the graph forks from the batch stream to every plan's stream, holds one
+// march step of each plan, and joins back, so the steps of all instances run
+// concurrently and the hardware block scheduler balances their uneven work
+// (per-column KT sub-cycle counts included: every column block is its own
+// block).  Other steps (a plan's first, last or partial step, screen and
+// source crossings) run eagerly on the plan's stream.  The graph is captured
+// again when the set of plans in it, or one of their generations, changes.
+// ---------------------------------------------------------------------------
+struct asg_batch {
+  std::vector<asg_plan*> plans;
+  cudaStream_t master = nullptr;
+  cudaEvent_t fork = nullptr, fork_cap = nullptr, ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> join, join_cap;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int> graph_set;
+  std::vector<long> graph_gens;
+  std::vector<long> graph_launches;  // [plan in set][kind]
+  bool use_graphs = true;
+  double run_ms = 0.0;
+};
+
+extern "C" int asg_batch_create(asg_plan* const* plans, int n, asg_batch** out) {
+  g_err.clear();
+  if (!plans || n <= 0 || !out) return fail(ASG_ERR_ARG, "bad argument");
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i]) return fail(ASG_ERR_ARG, "null plan %d", i);
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return fail(ASG_ERR_ARG, "plan %d appears twice", i);
+  }
+  asg_batch* b = new asg_batch();
+  b->plans.assign(plans, plans + n);
+  auto cleanup = [&](int code, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (b->master) cudaStreamDestroy(b->master);
+    for (cudaEvent_t ev : {b->fork, b->fork_cap, b->ev0, b->ev1})
+      if (ev) cudaEventDestroy(ev);
+    for (auto ev : b->join) cudaEventDestroy(ev);
+    for (auto ev : b->join_cap) cudaEventDestroy(ev);
+    delete b;
+    return fail(code, "%s: %s", what, cudaGetErrorString(e));
+  };
+  if (cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking) != cudaSuccess)
+    return cleanup(ASG_ERR_CUDA, "stream");
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork_cap, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+    return cleanup(ASG_ERR_CUDA, "events");
+  for (int i = 0; i < n; ++i) {
+    cudaEvent_t a, c;
+    if (cudaEventCreateWithFlags(&a, cudaEventDisableTiming) != cudaSuccess)
+      return cleanup(ASG_ERR_CUDA, "events");
+    b->join.push_back(a);
+    if (cudaEventCreateWithFlags(&c, cudaEventDisableTiming) != cudaSuccess)
+      return cleanup(ASG_ERR_CUDA, "events");
+    b->join_cap.push_back(c);
+  }
+  *out = b;
+  return ASG_OK;
+}
+
+extern "C" int asg_batch_destroy(asg_batch* b) {
+  if (!b) return ASG_OK;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaStreamSynchronize(b->master);
+  cudaStreamDestroy(b->master);
+  for (cudaEvent_t ev : {b->fork, b->fork_cap, b->ev0, b->ev1}) cudaEventDestroy(ev);
+  for (auto ev : b->join) cudaEventDestroy(ev);
+  for (auto ev : b->join_cap) cudaEventDestroy(ev);
+  delete b;
+  return ASG_OK;
+}
+
+extern "C" int asg_batch_set_graphs(asg_batch* b, int enable) {
+  if (!b) return fail(ASG_ERR_ARG, "null batch");
+  b->use_graphs = enable != 0;
+  return ASG_OK;
+}
+
+extern "C" int asg_batch_last_run_ms(asg_batch* b, double* ms) {
+  if (!b || !ms) return fail(ASG_ERR_ARG, "null argument");
+  *ms = b->run_ms;
+  return ASG_OK;
+}
+
+// the batch stream waits for the listed plans' streams
+static int batch_join(asg_batch* b, const std::vector<int>& set) {
+  for (int i : set) {
+    CK(cudaEventRecord(b->join[i], b->plans[i]->st));
+    CK(cudaStreamWaitEvent(b->master, b->join[i], 0));
+  }
+  return ASG_OK;
+}
+// the listed plans' streams wait for the batch stream
+static int batch_fork(asg_batch* b, const std::vector<int>& set) {
+  CK(cudaEventRecord(b->fork, b->master));
+  for (int i : set) CK(cudaStreamWaitEvent(b->plans[i]->st, b->fork, 0));
+  return ASG_OK;
+}
+
+static int batch_capture(asg_batch* b, const std::vector<int>& set,
+                         const std::vector<RunState>& rs, size_t k) {
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  std::vector<long> before(set.size() * ASG_NKINDS);
+  for (size_t j = 0; j < set.size(); ++j)
+    for (int q = 0; q < ASG_NKINDS; ++q) before[j * ASG_NKINDS + q] = b->plans[set[j]]->launches[q];
+  CK(cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal));
+  int st = ASG_OK;
+  if (cudaEventRecord(b->fork_cap, b->master) != cudaSuccess) st = ASG_ERR_CUDA;
+  for (int i : set) {
+    asg_plan* p = b->plans[i];
+    if (st == ASG_OK && cudaStreamWaitEvent(p->st, b->fork_cap, 0) != cudaSuccess) st = ASG_ERR_CUDA;
+    if (st == ASG_OK) {
+      const double dzs = rs[i].steps[k];
+      st = march_step(p, p->slot[0], dzs, step_btvd(p, dzs), 0, 0, false, false);
     }
-    scr.clear();
-    for (auto& sc : p->screens)
-      if (z < sc.z && sc.z <= z + dzs) scr.push_back(ScreenDev{sc.phase, sc.amp});
-    src.clear();
-    for (auto& so : p->sources)
-      if (z < so.z && so.z <= z + dzs) src.push_back(SourceEvent{so.map, so.val});
-    if (scr.size() > 64 || src.size() > 64)
-      return fail(ASG_ERR_ARG, "more than 64 screens or sources in one step");
-    if (!scr.empty()) CKS(h2d(p->d_screens, scr.data(), scr.size(), p->st));
-    if (!src.empty()) CKS(h2d(p->d_src, src.data(), src.size(), p->st));
-    const bool last = (k + 1 == steps.size());
-    const double norm_step = dzs / (p->cfg.c0 / p->cfg.f0);
-    const double btvd = fmax(1.0, 2.0 - p->cfg.adaptive_filter_strength * norm_step * 10);
-    const bool regular = p->use_graphs && !partial && scr.empty() && src.empty() && !last &&
-                         cb == nullptr && !p->prof;
-    if (regular) CKS(regular_step(p, *s, dzs, btvd, regular_seen));
-    else CKS(march_step(p, *s, dzs, btvd, (int)scr.size(), (int)src.size(), last, cb != nullptr));
-    zcum += dzs;
-    zsum.add(dzs);
-    p->zaxis.push_back(zcum);
+    // every stream that joined rejoins the batch stream, also after a failure
+    cudaEventRecord(b->join_cap[i], p->st);
+    cudaStreamWaitEvent(b->master, b->join_cap[i], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(b->master, &g);
+  if (st != ASG_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    if (st != ASG_OK) return g_err.empty() ? fail(st, "batch step capture failed") : st;
+    return fail(ASG_ERR_CUDA, "batch step capture: %s", cudaGetErrorString(e));
+  }
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e2 = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e2 != cudaSuccess)
+    return fail(ASG_ERR_CUDA, "batch graph instantiation: %s", cudaGetErrorString(e2));
+  b->graph = ex;
+  b->graph_set = set;
+  b->graph_gens.clear();
+  b->graph_launches.assign(set.size() * ASG_NKINDS, 0);
+  for (size_t j = 0; j < set.size(); ++j) {
+    asg_plan* p = b->plans[set[j]];
+    b->graph_gens.push_back(p->gen);
+    for (int q = 0; q < ASG_NKINDS; ++q) {
+      b->graph_launches[j * ASG_NKINDS + q] = p->launches[q] - before[j * ASG_NKINDS + q];
+      p->launches[q] = before[j * ASG_NKINDS + q];  // counted when the graph is launched
+    }
+  }
+  return ASG_OK;
+}
+
+extern "C" int asg_batch_run(asg_batch* b, const float* const* fields, const double* prop_dist,
+                             const double* dz, int* n_steps_out) {
+  g_err.clear();
+  if (!b || !fields || !prop_dist || !dz) return fail(ASG_ERR_ARG, "null argument");
+  const int n = (int)b->plans.size();
+  std::vector<RunState> rs(n);
+  std::vector<int> all(n);
+  size_t kmax = 0;
+  for (int i = 0; i < n; ++i) {
+    all[i] = i;
+    const int st = prepare_run(b->plans[i], fields[i], prop_dist[i], dz[i], rs[i]);
+    if (st != ASG_OK) {
+      for (int j = 0; j < n; ++j) cudaStreamSynchronize(b->plans[j]->st);
+      return st;
+    }
+    kmax = rs[i].steps.size() > kmax ? rs[i].steps.size() : kmax;
+  }
+  // the timed region starts once every plan is set up
+  CKS(batch_join(b, all));
+  CK(cudaEventRecord(b->ev0, b->master));
+  CKS(batch_fork(b, all));
+  std::vector<int> set;
+  for (size_t k = 0; k < kmax; ++k) {
+    set.clear();
+    for (int i = 0; i < n; ++i) {
+      if (k >= rs[i].steps.size()) continue;
+      asg_plan* p = b->plans[i];
+      if (b->use_graphs && step_is_regular(p, rs[i], k, false) && rs[i].regular_seen) {
+        set.push_back(i);
+      } else {
+        if (step_is_regular(p, rs[i], k, false)) rs[i].regular_seen = true;
+        CKS(eager_step(p, rs[i], k, false));
+      }
+    }
+    if (!set.empty()) {
+      bool same = b->graph != nullptr && b->graph_set == set;
+      for (size_t j = 0; same && j < set.size(); ++j)
+        same = b->graph_gens[j] == b->plans[set[j]]->gen;
+      CKS(batch_join(b, set));
+      if (!same) CKS(batch_capture(b, set, rs, k));
+      CK(cudaGraphLaunch(b->graph, b->master));
+      for (size_t j = 0; j < set.size(); ++j)
+        for (int q = 0; q < ASG_NKINDS; ++q)
+          b->plans[set[j]]->launches[q] += b->graph_launches[j * ASG_NKINDS + q];
+      CKS(batch_fork(b, set));
+    }
+    for (int i = 0; i < n; ++i)
+      if (k < rs[i].steps.size()) step_done(b->plans[i], rs[i], k);
+  }
+  CKS(batch_join(b, all));
+  CK(cudaEventRecord(b->ev1, b->master));
+  CK(cudaStreamSynchronize(b->master));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->run_ms = ms;
+  int first = ASG_OK;
+  std::string msg;
+  for (int i = 0; i < n; ++i) {
+    const int st = finish_run(b->plans[i], rs[i]);
+    if (n_steps_out) n_steps_out[i] = b->plans[i]->nsteps;
+    if (st != ASG_OK && first == ASG_OK) {
+      first = st;
+      msg = "instance " + std::to_string(i) + ": " + g_err;
+    }
+  }
+  if (first != ASG_OK) g_err = msg;
+  return first;
+}
+
+extern "C" int asg_run(asg_plan* p, const float* init, double prop_dist, double dz,
+                       asg_step_cb cb, void* user, int* n_steps_out) {
+  g_err.clear();
+  RunState rs;
+  CKS(prepare_run(p, init, prop_dist, dz, rs));
+  CK(cudaEventRecord(p->ev0, p->st));
+  for (size_t k = 0; k < rs.steps.size(); ++k) {
+    if (step_is_regular(p, rs, k, cb != nullptr))
+      CKS(regular_step(p, p->slot[0], rs.steps[k], step_btvd(p, rs.steps[k]), rs.regular_seen));
+    else
+      CKS(eager_step(p, rs, k, cb != nullptr));
+    step_done(p, rs, k);
     if (cb) {
       CK(cudaStreamSynchronize(p->st));
       CKS(status_to_error(p));
-      cb(user, (int)k, zsum.value(), p->real);
+      cb(user, (int)k, rs.zsum.value(), p->real);
     }
   }
   CK(cudaEventRecord(p->ev1, p->st));
   CK(cudaStreamSynchronize(p->st));
-  collect_kernel_times(p);
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, p->ev0, p->ev1));
   p->run_ms = ms;
-  p->nsteps = (int)steps.size();
+  const int st = finish_run(p, rs);
   if (n_steps_out) *n_steps_out = p->nsteps;
-  return status_to_error(p);
+  return st;
 }
 
 extern "C" int asg_get_outputs(asg_plan* p, float* field, float* pnp, float* ppp, float* pI,

@@ -259,6 +259,108 @@ def _torch_view(ptr, shape):
     return torch.as_tensor(_Dev(), device="cuda")
 
 
+def _prepared_plan(u0, params, kt_cfl_target=0.0, kt_max_subcycles=64):
+    """A plan with the step operators (regular and partial step), screens and
+    sources of one solve; returns (plan, dZ, step sequence)."""
+    dz = initial_step(u0, params)
+    steps = step_sequence(params.propDist, dz)
+    plan = Plan(u0.shape, params, kt_cfl_target=kt_cfl_target, kt_max_subcycles=kt_max_subcycles)
+    try:
+        plan.set_operators(0, dz)
+        partial = [s for s in steps if abs(s - dz) > 1e-15]
+        if partial:
+            plan.set_operators(1, partial[-1])
+        if params.phaseScreens is not None:
+            for scr in params.phaseScreens:
+                amp = scr[2] if len(scr) > 2 else None
+                plan.add_screen(scr[0], scr[1], amp)
+        if params.sourcePlanes is not None:
+            for z, plane in params.sourcePlanes:
+                plan.add_source(z, plane)
+    except Exception:
+        plan.close()
+        raise
+    return plan, dz, steps
+
+
+class Batch:
+    """Independent plans (grids of any size) marched together: every batch
+    step of the plans' regular steps is one CUDA-graph launch that forks to
+    all plans' streams (see asg_batch_run)."""
+
+    def __init__(self, plans):
+        self.lib = _lib.load()
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[p.h.value for p in self.plans])
+        h = C.c_void_p()
+        _lib.check(self.lib.asg_batch_create(arr, len(self.plans), C.byref(h)))
+        self.h = h
+
+    def set_graphs(self, enable: bool):
+        _lib.check(self.lib.asg_batch_set_graphs(self.h, int(enable)))
+
+    def run(self, fields, prop_dists, dzs):
+        n = len(self.plans)
+        us = [np.ascontiguousarray(f, dtype=np.float32) for f in fields]
+        for u, p in zip(us, self.plans):
+            assert u.shape == p.shape
+        fp = (C.POINTER(C.c_float) * n)(*[_lib.fptr(u) for u in us])
+        pd = (C.c_double * n)(*[float(x) for x in prop_dists])
+        dd = (C.c_double * n)(*[float(x) for x in dzs])
+        ns = (C.c_int * n)()
+        _lib.check(self.lib.asg_batch_run(self.h, fp, pd, dd, ns))
+        for p, k in zip(self.plans, ns):
+            p.nsteps = k
+        return list(ns)
+
+    def last_run_ms(self):
+        v = C.c_double(0)
+        _lib.check(self.lib.asg_batch_last_run_ms(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.asg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_batch(initial_fields, params_list, kt_cfl_target: float = 0.0,
+                kt_max_subcycles: int = 64, return_timing: bool = False):
+    """`angular_spectrum_solve` of many independent instances (uneven grids
+    allowed) in one batched march.  Returns one output tuple per instance,
+    each exactly as `angular_spectrum_solve` returns it (and the device time
+    of the march in ms with return_timing)."""
+    if len(initial_fields) != len(params_list):
+        raise ValueError("one parameter set per initial field")
+    plans, dzs, us = [], [], []
+    try:
+        for f, prm in zip(initial_fields, params_list):
+            u0 = np.ascontiguousarray(f, dtype=np.float32)
+            if u0.ndim != 3:
+                raise ValueError("initial_field must be (nX, nY, nT)")
+            plan, dz, _ = _prepared_plan(u0, prm, kt_cfl_target, kt_max_subcycles)
+            plans.append(plan)
+            dzs.append(dz)
+            us.append(u0)
+        batch = Batch(plans)
+        try:
+            batch.run(us, [prm.propDist for prm in params_list], dzs)
+            outs = [p.outputs() for p in plans]
+            ms = batch.last_run_ms()
+        finally:
+            batch.close()
+        return (outs, ms) if return_timing else outs
+    finally:
+        for p in plans:
+            p.close()
+
+
 def angular_spectrum_solve(
         initial_field: np.ndarray,
         params: SolverParams,
@@ -284,21 +386,8 @@ def angular_spectrum_solve(
     if u0.ndim != 3:
         raise ValueError("initial_field must be (nX, nY, nT)")
     nX, nY, nT = u0.shape
-    dz = initial_step(initial_field, params)
-    steps = step_sequence(params.propDist, dz)
-    plan = Plan(u0.shape, params)
+    plan, dz, steps = _prepared_plan(u0, params)
     try:
-        plan.set_operators(0, dz)
-        partial = [s for s in steps if abs(s - dz) > 1e-15]
-        if partial:
-            plan.set_operators(1, partial[-1])
-        if params.phaseScreens is not None:
-            for scr in params.phaseScreens:
-                amp = scr[2] if len(scr) > 2 else None
-                plan.add_screen(scr[0], scr[1], amp)
-        if params.sourcePlanes is not None:
-            for z, plane in params.sourcePlanes:
-                plan.add_source(z, plane)
         cb = None
         if per_step_callback is not None:
             def cb(user, step, z, ptr):

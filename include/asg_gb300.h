@@ -161,6 +161,25 @@ int asg_kernel_stats(asg_plan* plan, double* ms, long* launches, int nkinds);
  * counterpart in the reference. */
 int asg_set_graphs(asg_plan* plan, int enable);
 
+/* Batched march of independent plans (no counterpart in the reference, which
+ * solves one instance per call).  Plans may have different grids and options;
+ * each keeps its own operators, screens, sources and outputs (asg_get_outputs
+ * per plan after the run).  Step k of all plans is issued together: the
+ * plans' regular steps as one CUDA-graph launch forking to every plan's
+ * stream, the others eagerly.  A plan belongs to at most one batch at a time
+ * and must not run on its own while the batch runs. */
+typedef struct asg_batch asg_batch;
+int asg_batch_create(asg_plan* const* plans, int n, asg_batch** out);
+int asg_batch_destroy(asg_batch* batch);
+int asg_batch_set_graphs(asg_batch* batch, int enable);
+/* fields[i]: host nX*nY*nT float32 of plan i; prop_dist[i], dz[i] as asg_run;
+ * n_steps_out[i] receives each plan's step count.  Returns the first error of
+ * any plan (its index in the message). */
+int asg_batch_run(asg_batch* batch, const float* const* fields, const double* prop_dist,
+                  const double* dz, int* n_steps_out);
+/* Device time of the last batched march (all plans' steps), milliseconds. */
+int asg_batch_last_run_ms(asg_batch* batch, double* ms);
+
 /* Launch shapes of a plan (no counterpart in the reference: its XLA program
  * has no tunable launch shapes). 0 in a field selects the built-in default. */
 typedef struct {
