@@ -27,6 +27,8 @@ EXPORTED = [
     "asg_kernel_stats", "asg_flux_columns_device", "asg_get_tuning", "asg_set_tuning",
     "asg_autotune", "asg_set_graphs", "asg_batch_create", "asg_batch_destroy",
     "asg_batch_set_graphs", "asg_batch_run", "asg_batch_last_run_ms",
+    "asg_net_param_count", "asg_net_create", "asg_net_destroy", "asg_net_set_params",
+    "asg_net_get_params", "asg_net_forward", "asg_net_train_step",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -116,6 +118,13 @@ def load(require_device: bool = True):
     lib.asg_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_autotune.argtypes = [P, F, C.c_double, C.c_int, C.POINTER(Tuning)]
     lib.asg_set_graphs.argtypes = [P, C.c_int]
+    lib.asg_net_param_count.argtypes = []
+    lib.asg_net_create.argtypes = [C.POINTER(P)]
+    lib.asg_net_destroy.argtypes = [P]
+    lib.asg_net_set_params.argtypes = [P, F, C.c_int]
+    lib.asg_net_get_params.argtypes = [P, F, C.c_int]
+    lib.asg_net_forward.argtypes = [P, P, P, C.c_int, C.c_int, P]
+    lib.asg_net_train_step.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_float, _DP, F]
     lib.asg_batch_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.asg_batch_destroy.argtypes = [P]
     lib.asg_batch_set_graphs.argtypes = [P, C.c_int]

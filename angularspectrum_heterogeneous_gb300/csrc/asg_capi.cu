@@ -1843,6 +1843,8 @@ extern "C" int asg_flux_columns_device(const float* d_in, float* d_out, int ncol
   return ASG_OK;
 }
 
+int asg_fail_message(int code, const char* msg) { return fail(code, "%s", msg); }
+
 extern "C" const char* asg_last_error(void) { return g_err.c_str(); }
 
 extern "C" const char* asg_version(void) {

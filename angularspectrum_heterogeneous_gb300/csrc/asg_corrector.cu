@@ -1,0 +1,620 @@
+// Learned KT corrector: a 1-D convolutional network along t that corrects one
+// coarse KT step of a column towards the fully sub-cycled KT step.
+//
+//   h1 = GELU(conv(x,  W1[64,1,5])  + b1)      CUDA cores
+//   h2 = GELU(conv(h1, W2[64,64,5]) + b2)      BF16 tensor cores, FP32 accumulation
+//   h3 = GELU(conv(h2, W3[64,64,5]) + b3)      BF16 tensor cores, FP32 accumulation
+//   y  =      conv(h3, W4[1,64,5])  + b4       CUDA cores
+//   conv(x, W)[o, t] = sum_i sum_j W[o, i, j] x[i, t + j - 2], zero outside the column
+//
+// The reference solver has no learned part; its KT scheme (_kt_flux /
+// _kt_flux_adaptive, angular_spectrum_solver.py:833-859) produces the
+// training targets through the column kernels of this library.
+//
+// Data layout: a batch of ncols columns of nT samples (nT % 64 == 0), position
+// pos = column * nT + t.  Activations are position-major [pos][64 channels]
+// (BF16, 128 B per position); pre-activations z are kept in FP32 for the
+// backward pass.  Parameters live in one FP32 vector theta (layout below);
+// the two 64x64 layers are packed to BF16 GEMM operands Wg[o][j*64 + i] (and
+// their transposes for the backward data pass) after every update.
+//
+// The 64x64 layers are GEMMs with M = 64 output channels, N = positions,
+// K = 5 taps x 64 input channels, issued as mma.sync.m16n8k16 BF16 tiles.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "asg_internal.h"
+
+namespace {
+
+typedef unsigned short bf16_t;  // raw bfloat16 bits
+
+constexpr int NCH = 64, KT5 = 5, KDIM = NCH * KT5;  // 320
+// theta layout (floats)
+constexpr int OFF_W1 = 0;                     // [64][5]        (o, j)
+constexpr int OFF_B1 = OFF_W1 + NCH * KT5;    // [64]
+constexpr int OFF_W2 = OFF_B1 + NCH;          // [64][64][5]    (o, i, j)
+constexpr int OFF_B2 = OFF_W2 + NCH * KDIM;
+constexpr int OFF_W3 = OFF_B2 + NCH;
+constexpr int OFF_B3 = OFF_W3 + NCH * KDIM;
+constexpr int OFF_W4 = OFF_B3 + NCH;          // [64][5]        (i, j)
+constexpr int OFF_B4 = OFF_W4 + NCH * KT5;    // [1]
+constexpr int NPARAM = OFF_B4 + 1;            // 41793
+
+__device__ __forceinline__ bf16_t f2bf(float f) {
+  // round to nearest even (finite inputs; NaN stays NaN)
+  unsigned u = __float_as_uint(f);
+  if ((u & 0x7f800000u) == 0x7f800000u) return (bf16_t)((u >> 16) | ((u & 0xffffu) ? 0x40u : 0u));
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (bf16_t)(u >> 16);
+}
+__device__ __forceinline__ float bf2f(bf16_t h) { return __uint_as_float(((unsigned)h) << 16); }
+
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad_f(float z) {
+  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2,
+                                         unsigned a3, unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// ---------------------------------------------------------------------------
+// 64 -> 64 channel convolution as a tensor-core GEMM.
+//   acc[pos][o] = sum_{j,i} Wg[o][j*64 + i] X[pos + j - 2][i]   (zero outside the column)
+// MODE 0 (forward):  z = acc + bias[o];  Z[pos][o] = z (if Z), H[pos][o] = bf16(GELU(z))
+// MODE 1 (backward data): d = acc * GELU'(Zin[pos][o]);  H[pos][o] = bf16(d)
+// A block of 4 warps owns 64 positions x 64 channels per tile (persistent over
+// tiles); warp w computes positions w*16 .. w*16+15 for all 64 channels.
+// ---------------------------------------------------------------------------
+constexpr int WS = KDIM + 8;   // row stride of the weight tile (bf16): conflict-free fragments
+constexpr int XS = NCH + 8;    // row stride of the activation tile
+constexpr int TP = 64;         // positions per tile
+constexpr size_t CONV_SMEM = (size_t)(NCH * WS + (TP + 4) * XS) * sizeof(bf16_t);
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_conv64(const bf16_t* __restrict__ X,
+                                                const bf16_t* __restrict__ Wg,
+                                                const float* __restrict__ bias,
+                                                const float* __restrict__ Zin,
+                                                float* __restrict__ Zout,
+                                                bf16_t* __restrict__ H, int npos, int nT) {
+  extern __shared__ uint4 smem_u4[];
+  bf16_t* Ws = reinterpret_cast<bf16_t*>(smem_u4);
+  bf16_t* Xs = Ws + NCH * WS;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  // weights once per block: 64 rows of 320 bf16 = 40 uint4 each
+  for (int i = tid; i < NCH * (KDIM / 8); i += blockDim.x) {
+    const int o = i / (KDIM / 8), c = i - o * (KDIM / 8);
+    *reinterpret_cast<uint4*>(Ws + o * WS + c * 8) =
+        *reinterpret_cast<const uint4*>(Wg + (size_t)o * KDIM + c * 8);
+  }
+  const int ntiles = npos / TP;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int pos0 = tile * TP;
+    const int cbeg = (pos0 / nT) * nT, cend = cbeg + nT;
+    __syncthreads();  // previous tile's readers are done (and the weights are in)
+    for (int i = tid; i < (TP + 4) * (NCH / 8); i += blockDim.x) {
+      const int r = i / (NCH / 8), c = i - r * (NCH / 8);
+      const int pos = pos0 - 2 + r;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (pos >= cbeg && pos < cend) v = *reinterpret_cast<const uint4*>(X + (size_t)pos * NCH + c * 8);
+      *reinterpret_cast<uint4*>(Xs + r * XS + c * 8) = v;
+    }
+    __syncthreads();
+    float acc[4][2][4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int n = 0; n < 2; ++n)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
+    const int nb = warp * 16;
+#pragma unroll 1
+    for (int j = 0; j < KT5; ++j) {
+#pragma unroll
+      for (int cb = 0; cb < 4; ++cb) {
+        const int k0 = j * NCH + cb * 16;
+        unsigned b[2][2];
+#pragma unroll
+        for (int n = 0; n < 2; ++n) {
+          const bf16_t* xr = Xs + (nb + n * 8 + gid + j) * XS + cb * 16 + tig * 2;
+          b[n][0] = *reinterpret_cast<const unsigned*>(xr);
+          b[n][1] = *reinterpret_cast<const unsigned*>(xr + 8);
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const bf16_t* wr = Ws + (m * 16 + gid) * WS + k0 + tig * 2;
+          const unsigned a0 = *reinterpret_cast<const unsigned*>(wr);
+          const unsigned a1 = *reinterpret_cast<const unsigned*>(wr + 8 * WS);
+          const unsigned a2 = *reinterpret_cast<const unsigned*>(wr + 8);
+          const unsigned a3 = *reinterpret_cast<const unsigned*>(wr + 8 * WS + 8);
+#pragma unroll
+          for (int n = 0; n < 2; ++n) mma_bf16(acc[m][n], a0, a1, a2, a3, b[n][0], b[n][1]);
+        }
+      }
+    }
+    // epilogue: acc[m][n][q] -> channel o = m*16 + gid (+8 for q >= 2),
+    //           position nb + n*8 + tig*2 (+1 for odd q)
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int n = 0; n < 2; ++n)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int o = m * 16 + gid + (q >= 2 ? 8 : 0);
+          const size_t pos = (size_t)pos0 + nb + n * 8 + tig * 2 + (q & 1);
+          const size_t idx = pos * NCH + o;
+          if (MODE == 0) {
+            const float z = acc[m][n][q] + bias[o];
+            if (Zout) Zout[idx] = z;
+            H[idx] = f2bf(gelu_f(z));
+          } else {
+            H[idx] = f2bf(acc[m][n][q] * gelu_grad_f(Zin[idx]));
+          }
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradient of a 64 -> 64 layer:
+//   dW[o][i][j] += sum_pos D[pos][o] X[pos + j - 2][i]
+// GEMM with M = o (64), N = (j, i) (320, split in 4 slabs of 80 over
+// blockIdx.y), K = positions (64 per chunk).  Tiles are staged
+// channel-major so that A fragments pair consecutive positions.
+// ---------------------------------------------------------------------------
+constexpr int WG_SLAB = 80;
+constexpr int DT_S = TP + 8;       // stride of the staged D^T tile [64][TP]
+constexpr int XT_S = TP + 4 + 4;   // stride of the staged X^T tile [64][TP + 4]
+constexpr size_t WGRAD_SMEM = (size_t)(NCH * DT_S + NCH * XT_S) * sizeof(bf16_t);
+
+__global__ void __launch_bounds__(128) k_conv64_wgrad(const bf16_t* __restrict__ D,
+                                                      const bf16_t* __restrict__ X,
+                                                      float* __restrict__ dW, int npos, int nT) {
+  extern __shared__ uint4 smem_u4[];
+  bf16_t* Dt = reinterpret_cast<bf16_t*>(smem_u4);
+  bf16_t* Xt = Dt + NCH * DT_S;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int slab = blockIdx.y;      // n-range [slab*80, +80)
+  const int m0 = warp * 16;         // output channels of this warp
+  float acc[10][4];
+#pragma unroll
+  for (int n = 0; n < 10; ++n)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[n][q] = 0.f;
+  const int nchunks = npos / TP;
+  for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const int pos0 = ch * TP;
+    const int cbeg = (pos0 / nT) * nT, cend = cbeg + nT;
+    __syncthreads();
+    for (int i = tid; i < TP * NCH; i += blockDim.x) {
+      const int p = i / NCH, o = i - p * NCH;
+      Dt[o * DT_S + p] = D[(size_t)(pos0 + p) * NCH + o];
+    }
+    for (int i = tid; i < (TP + 4) * NCH; i += blockDim.x) {
+      const int r = i / NCH, c = i - r * NCH;
+      const int pos = pos0 - 2 + r;
+      Xt[c * XT_S + r] = (pos >= cbeg && pos < cend) ? X[(size_t)pos * NCH + c] : (bf16_t)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < TP / 16; ++ks) {
+      const int p0 = ks * 16;
+      const bf16_t* ar = Dt + (m0 + gid) * DT_S + p0 + tig * 2;
+      const unsigned a0 = *reinterpret_cast<const unsigned*>(ar);
+      const unsigned a1 = *reinterpret_cast<const unsigned*>(ar + 8 * DT_S);
+      const unsigned a2 = *reinterpret_cast<const unsigned*>(ar + 8);
+      const unsigned a3 = *reinterpret_cast<const unsigned*>(ar + 8 * DT_S + 8);
+#pragma unroll
+      for (int n = 0; n < 10; ++n) {
+        const int kk = slab * WG_SLAB + n * 8 + gid;  // column (j, i) of this lane's B values
+        const int j = kk / NCH, i = kk - j * NCH;
+        // B[k = position][n = (j, i)] = X[p + j - 2][i] = Xt[i][p + j]
+        const bf16_t* xr = Xt + i * XT_S + p0 + tig * 2 + j;
+        const unsigned b0 = (unsigned)xr[0] | ((unsigned)xr[1] << 16);
+        const unsigned b1 = (unsigned)xr[8] | ((unsigned)xr[9] << 16);
+        mma_bf16(acc[n], a0, a1, a2, a3, b0, b1);
+      }
+    }
+  }
+  // acc[n][q]: o = m0 + gid (+8 for q >= 2), k = slab*80 + n*8 + tig*2 (+1 for odd q)
+#pragma unroll
+  for (int n = 0; n < 10; ++n)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int o = m0 + gid + (q >= 2 ? 8 : 0);
+      const int kk = slab * WG_SLAB + n * 8 + tig * 2 + (q & 1);
+      const int j = kk / NCH, i = kk - j * NCH;
+      atomicAdd(dW + (size_t)o * KDIM + i * KT5 + j, acc[n][q]);
+    }
+}
+
+// bias gradient: db[o] += sum_pos D[pos][o]
+__global__ void k_bias_grad(const bf16_t* __restrict__ D, float* __restrict__ db, int npos) {
+  __shared__ float part[256];
+  const int o = threadIdx.x & 63, lane4 = threadIdx.x >> 6;  // 4 position lanes x 64 channels
+  float s = 0.f;
+  for (int p = blockIdx.x * 4 + lane4; p < npos; p += gridDim.x * 4) s += bf2f(D[(size_t)p * NCH + o]);
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x < 64) atomicAdd(db + o, part[o] + part[o + 64] + part[o + 128] + part[o + 192]);
+}
+
+// ---------------------------------------------------------------------------
+// first layer (1 -> 64) and its weight gradient, last layer (64 -> 1) with the
+// loss, and its backward: CUDA cores
+// ---------------------------------------------------------------------------
+__global__ void k_layer1_fwd(const float* __restrict__ x, const float* __restrict__ th,
+                             float* __restrict__ Z, bf16_t* __restrict__ H, int npos, int nT) {
+  const size_t n = (size_t)npos * NCH;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int pos = (int)(idx / NCH), o = (int)(idx - (size_t)pos * NCH);
+    const int t = pos % nT;
+    float z = th[OFF_B1 + o];
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) {
+      const int tt = t + j - 2;
+      if (tt >= 0 && tt < nT) z = fmaf(th[OFF_W1 + o * KT5 + j], x[pos + j - 2], z);
+    }
+    if (Z) Z[idx] = z;
+    H[idx] = f2bf(gelu_f(z));
+  }
+}
+
+// y = b4 + sum_{j,i} W4[i][j] h3[pos + j - 2][i]; with a target: the masked
+// squared error goes to loss_acc[0] (sum) and dy = 2 (y - target) mask / nmask
+__global__ void k_layer4_fwd(const bf16_t* __restrict__ H3, const float* __restrict__ th,
+                             float* __restrict__ y, const float* __restrict__ target,
+                             const float* __restrict__ mask, float inv_nmask,
+                             float* __restrict__ dy, double* __restrict__ loss_acc, int npos,
+                             int nT) {
+  __shared__ float w4[NCH * KT5];
+  __shared__ double red[8];
+  for (int i = threadIdx.x; i < NCH * KT5; i += blockDim.x) w4[i] = th[OFF_W4 + i];
+  __syncthreads();
+  double lsum = 0.0;
+  for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < npos; pos += gridDim.x * blockDim.x) {
+    const int t = pos % nT;
+    float v = th[OFF_B4];
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) {
+      const int tt = t + j - 2;
+      if (tt < 0 || tt >= nT) continue;
+      const uint4* hr = reinterpret_cast<const uint4*>(H3 + (size_t)(pos + j - 2) * NCH);
+#pragma unroll
+      for (int c = 0; c < NCH / 8; ++c) {
+        const uint4 q = hr[c];
+        const unsigned w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = c * 8 + e * 2;
+          v = fmaf(w4[i * KT5 + j], bf2f((bf16_t)(w[e] & 0xffffu)), v);
+          v = fmaf(w4[(i + 1) * KT5 + j], bf2f((bf16_t)(w[e] >> 16)), v);
+        }
+      }
+    }
+    y[pos] = v;
+    if (target) {
+      const float r = (v - target[pos]) * mask[pos];
+      lsum += (double)r * (double)r;
+      dy[pos] = 2.f * r * inv_nmask;
+    }
+  }
+  if (target) {
+    lsum = warp_sum(lsum);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      atomicAdd(loss_acc, s);
+    }
+  }
+}
+
+// backward of the last layer: dz3[pos][i] = (sum_j W4[i][j] dy[pos - j + 2]) GELU'(z3),
+// dW4[i][j] += sum_pos dy[pos] h3[pos + j - 2][i], db4 += sum dy
+__global__ void k_layer4_bwd(const float* __restrict__ dy, const bf16_t* __restrict__ H3,
+                             const float* __restrict__ Z3, const float* __restrict__ th,
+                             bf16_t* __restrict__ DZ3, float* __restrict__ g, int npos, int nT) {
+  __shared__ float gw[NCH * KT5];
+  __shared__ float gb;
+  for (int i = threadIdx.x; i < NCH * KT5; i += blockDim.x) gw[i] = 0.f;
+  if (threadIdx.x == 0) gb = 0.f;
+  __syncthreads();
+  const int i = threadIdx.x & 63, pl = threadIdx.x >> 6, npl = blockDim.x >> 6;
+  float accw[KT5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float accb = 0.f;
+  for (int pos = blockIdx.x * npl + pl; pos < npos; pos += gridDim.x * npl) {
+    const int t = pos % nT;
+    float d = 0.f;
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) {
+      const int tt = t - j + 2;
+      if (tt >= 0 && tt < nT) d = fmaf(th[OFF_W4 + i * KT5 + j], dy[pos - j + 2], d);
+      const int ts = t + j - 2;
+      if (ts >= 0 && ts < nT) accw[j] = fmaf(dy[pos], bf2f(H3[(size_t)(pos + j - 2) * NCH + i]), accw[j]);
+    }
+    const size_t idx = (size_t)pos * NCH + i;
+    DZ3[idx] = f2bf(d * gelu_grad_f(Z3[idx]));
+    if (i == 0) accb += dy[pos];
+  }
+#pragma unroll
+  for (int j = 0; j < KT5; ++j) atomicAdd(&gw[i * KT5 + j], accw[j]);
+  if (i == 0) atomicAdd(&gb, accb);
+  __syncthreads();
+  for (int k = threadIdx.x; k < NCH * KT5; k += blockDim.x) atomicAdd(g + OFF_W4 + k, gw[k]);
+  if (threadIdx.x == 0) atomicAdd(g + OFF_B4, gb);
+}
+
+// first-layer weight gradient: dW1[o][j] += sum_pos dz1[pos][o] x[pos + j - 2]; db1[o]
+__global__ void k_layer1_bwd(const bf16_t* __restrict__ DZ1, const float* __restrict__ x,
+                             float* __restrict__ g, int npos, int nT) {
+  const int o = threadIdx.x & 63, pl = threadIdx.x >> 6, npl = blockDim.x >> 6;
+  float accw[KT5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float accb = 0.f;
+  for (int pos = blockIdx.x * npl + pl; pos < npos; pos += gridDim.x * npl) {
+    const int t = pos % nT;
+    const float d = bf2f(DZ1[(size_t)pos * NCH + o]);
+    accb += d;
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) {
+      const int tt = t + j - 2;
+      if (tt >= 0 && tt < nT) accw[j] = fmaf(d, x[pos + j - 2], accw[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < KT5; ++j) atomicAdd(g + OFF_W1 + o * KT5 + j, accw[j]);
+  atomicAdd(g + OFF_B1 + o, accb);
+}
+
+// theta -> BF16 GEMM operands: Wg[o][j*64+i] = W[o][i][j],
+// WgT[i][j*64+o] = W[o][i][4-j] (the transposed convolution as a forward one)
+__global__ void k_pack(const float* __restrict__ th, bf16_t* __restrict__ Wg2,
+                       bf16_t* __restrict__ Wt2, bf16_t* __restrict__ Wg3,
+                       bf16_t* __restrict__ Wt3) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < NCH * KDIM;
+       idx += gridDim.x * blockDim.x) {
+    const int r = idx / KDIM, k = idx - r * KDIM;
+    const int j = k / NCH, c = k - j * NCH;
+    // Wg[r = o][k = j*64 + c = i]
+    Wg2[idx] = f2bf(th[OFF_W2 + r * KDIM + c * KT5 + j]);
+    Wg3[idx] = f2bf(th[OFF_W3 + r * KDIM + c * KT5 + j]);
+    // Wt[r = i][k = j*64 + c = o] = W[o][i][4 - j]
+    Wt2[idx] = f2bf(th[OFF_W2 + c * KDIM + r * KT5 + (KT5 - 1 - j)]);
+    Wt3[idx] = f2bf(th[OFF_W3 + c * KDIM + r * KT5 + (KT5 - 1 - j)]);
+  }
+}
+
+// Adam (FP32 master weights)
+__global__ void k_adam(float* __restrict__ th, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, int n, float lr, float b1, float b2,
+                       float c1, float c2, float eps) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    th[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// net object
+// ---------------------------------------------------------------------------
+struct asg_net {
+  float *theta = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
+  bf16_t *wg2 = nullptr, *wt2 = nullptr, *wg3 = nullptr, *wt3 = nullptr;
+  double* loss = nullptr;
+  int adam_t = 0;
+  // activations of the largest batch seen
+  size_t cap = 0;
+  float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *dy = nullptr, *yb = nullptr;
+  bf16_t *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *d1 = nullptr, *d2 = nullptr;
+  int nsm = 152;
+};
+
+static int net_fail(int code, const char* msg) { return asg_fail_message(code, msg); }
+
+static void net_free_acts(asg_net* n) {
+  void* ps[] = {n->z1, n->z2, n->z3, n->dy, n->yb, n->h1, n->h2, n->h3, n->d1, n->d2};
+  for (void* p : ps) cudaFree(p);
+  n->z1 = n->z2 = n->z3 = n->dy = n->yb = nullptr;
+  n->h1 = n->h2 = n->h3 = n->d1 = n->d2 = nullptr;
+  n->cap = 0;
+}
+
+static int net_ensure(asg_net* n, size_t npos) {
+  if (n->cap >= npos) return ASG_OK;
+  net_free_acts(n);
+  const size_t a = npos * NCH;
+  bool ok = cudaMalloc(&n->z1, a * 4) == cudaSuccess && cudaMalloc(&n->z2, a * 4) == cudaSuccess &&
+            cudaMalloc(&n->z3, a * 4) == cudaSuccess && cudaMalloc(&n->dy, npos * 4) == cudaSuccess &&
+            cudaMalloc(&n->yb, npos * 4) == cudaSuccess &&
+            cudaMalloc(&n->h1, a * 2) == cudaSuccess && cudaMalloc(&n->h2, a * 2) == cudaSuccess &&
+            cudaMalloc(&n->h3, a * 2) == cudaSuccess && cudaMalloc(&n->d1, a * 2) == cudaSuccess &&
+            cudaMalloc(&n->d2, a * 2) == cudaSuccess;
+  if (!ok) {
+    net_free_acts(n);
+    return net_fail(ASG_ERR_NOMEM, "corrector activations: cudaMalloc failed");
+  }
+  n->cap = npos;
+  return ASG_OK;
+}
+
+static int net_pack(asg_net* n, cudaStream_t st) {
+  k_pack<<<80, 256, 0, st>>>(n->theta, n->wg2, n->wt2, n->wg3, n->wt3);
+  return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "pack launch");
+}
+
+static int conv_smem_attr() {
+  static bool done = false;
+  if (done) return ASG_OK;
+  if (cudaFuncSetAttribute(k_conv64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv64_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WGRAD_SMEM) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "corrector kernels: shared-memory attribute");
+  done = true;
+  return ASG_OK;
+}
+
+// forward of the whole network: x [npos] -> y [npos] (z's kept when keep_z)
+static int net_forward(asg_net* n, const float* x, float* y, const float* target,
+                       const float* mask, float inv_nmask, int npos, int nT, bool keep_z,
+                       cudaStream_t st) {
+  CKS_NET(conv_smem_attr());
+  const int tiles = npos / TP;
+  const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
+  k_layer1_fwd<<<4 * n->nsm, 256, 0, st>>>(x, n->theta, keep_z ? n->z1 : nullptr, n->h1, npos, nT);
+  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(n->h1, n->wg2, n->theta + OFF_B2, nullptr,
+                                             keep_z ? n->z2 : nullptr, n->h2, npos, nT);
+  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(n->h2, n->wg3, n->theta + OFF_B3, nullptr,
+                                             keep_z ? n->z3 : nullptr, n->h3, npos, nT);
+  k_layer4_fwd<<<4 * n->nsm, 256, 0, st>>>(n->h3, n->theta, y, target, mask, inv_nmask, n->dy,
+                                           n->loss, npos, nT);
+  return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "forward launch");
+}
+
+static int net_backward(asg_net* n, const float* x, int npos, int nT, cudaStream_t st) {
+  const int tiles = npos / TP;
+  const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
+  const int gw = tiles < n->nsm ? tiles : n->nsm;
+  // last layer: dW4, db4, dz3 -> d2
+  k_layer4_bwd<<<2 * n->nsm, 256, 0, st>>>(n->dy, n->h3, n->z3, n->theta, n->d2, n->grad, npos, nT);
+  // layer 3: dW3 (dz3, h2), db3, dz2 = (W3^T * dz3) GELU'(z2) -> d1
+  k_conv64_wgrad<<<dim3(gw, KDIM / WG_SLAB), 128, WGRAD_SMEM, st>>>(n->d2, n->h2, n->grad + OFF_W3, npos, nT);
+  k_bias_grad<<<2 * n->nsm, 256, 0, st>>>(n->d2, n->grad + OFF_B3, npos);
+  k_conv64<1><<<gconv, 128, CONV_SMEM, st>>>(n->d2, n->wt3, nullptr, n->z2, nullptr, n->d1, npos, nT);
+  // layer 2: dW2 (dz2, h1), db2, dz1 = (W2^T * dz2) GELU'(z1) -> d2
+  k_conv64_wgrad<<<dim3(gw, KDIM / WG_SLAB), 128, WGRAD_SMEM, st>>>(n->d1, n->h1, n->grad + OFF_W2, npos, nT);
+  k_bias_grad<<<2 * n->nsm, 256, 0, st>>>(n->d1, n->grad + OFF_B2, npos);
+  k_conv64<1><<<gconv, 128, CONV_SMEM, st>>>(n->d1, n->wt2, nullptr, n->z1, nullptr, n->d2, npos, nT);
+  // layer 1
+  k_layer1_bwd<<<2 * n->nsm, 256, 0, st>>>(n->d2, x, n->grad, npos, nT);
+  return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "backward launch");
+}
+
+extern "C" int asg_net_param_count(void) { return NPARAM; }
+
+extern "C" int asg_net_create(asg_net** out) {
+  if (!out) return net_fail(ASG_ERR_ARG, "null argument");
+  asg_net* n = new asg_net();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n->nsm, cudaDevAttrMultiProcessorCount, dev);
+  bool ok = cudaMalloc(&n->theta, NPARAM * 4) == cudaSuccess &&
+            cudaMalloc(&n->adam_m, NPARAM * 4) == cudaSuccess &&
+            cudaMalloc(&n->adam_v, NPARAM * 4) == cudaSuccess &&
+            cudaMalloc(&n->grad, NPARAM * 4) == cudaSuccess &&
+            cudaMalloc(&n->wg2, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wt2, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wg3, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wt3, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->loss, sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    asg_net_destroy(n);
+    return net_fail(ASG_ERR_NOMEM, "corrector parameters: cudaMalloc failed");
+  }
+  cudaMemset(n->theta, 0, NPARAM * 4);
+  cudaMemset(n->adam_m, 0, NPARAM * 4);
+  cudaMemset(n->adam_v, 0, NPARAM * 4);
+  *out = n;
+  return net_pack(n, 0) == ASG_OK && cudaDeviceSynchronize() == cudaSuccess
+             ? ASG_OK : net_fail(ASG_ERR_CUDA, "corrector set-up");
+}
+
+extern "C" int asg_net_destroy(asg_net* n) {
+  if (!n) return ASG_OK;
+  net_free_acts(n);
+  void* ps[] = {n->theta, n->adam_m, n->adam_v, n->grad, n->wg2, n->wt2, n->wg3, n->wt3, n->loss};
+  for (void* p : ps) cudaFree(p);
+  delete n;
+  return ASG_OK;
+}
+
+extern "C" int asg_net_set_params(asg_net* n, const float* theta, int count) {
+  if (!n || !theta || count != NPARAM) return net_fail(ASG_ERR_ARG, "bad parameter vector");
+  if (cudaMemcpy(n->theta, theta, NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "parameter upload");
+  cudaMemset(n->adam_m, 0, NPARAM * 4);
+  cudaMemset(n->adam_v, 0, NPARAM * 4);
+  n->adam_t = 0;
+  CKS_NET(net_pack(n, 0));
+  return cudaDeviceSynchronize() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "pack");
+}
+
+extern "C" int asg_net_get_params(asg_net* n, float* theta, int count) {
+  if (!n || !theta || count != NPARAM) return net_fail(ASG_ERR_ARG, "bad parameter vector");
+  return cudaMemcpy(theta, n->theta, NPARAM * 4, cudaMemcpyDeviceToHost) == cudaSuccess
+             ? ASG_OK : net_fail(ASG_ERR_CUDA, "parameter download");
+}
+
+static int check_batch(int ncols, int nT) {
+  if (ncols <= 0 || nT < 64 || nT % TP != 0)
+    return net_fail(ASG_ERR_SHAPE, "corrector batches need nT a multiple of 64");
+  return ASG_OK;
+}
+
+extern "C" int asg_net_forward(asg_net* n, const float* d_x, float* d_y, int ncols, int nT,
+                               void* stream) {
+  if (!n || !d_x || !d_y) return net_fail(ASG_ERR_ARG, "null argument");
+  CKS_NET(check_batch(ncols, nT));
+  const size_t npos = (size_t)ncols * nT;
+  CKS_NET(net_ensure(n, npos));
+  return net_forward(n, d_x, d_y, nullptr, nullptr, 0.f, (int)npos, nT, false,
+                     static_cast<cudaStream_t>(stream));
+}
+
+// One training step on a device batch: loss (masked MSE) and gradients; with
+// lr > 0 an Adam update follows.  h_grad (host, NPARAM floats) receives the
+// gradients when not null.
+extern "C" int asg_net_train_step(asg_net* n, const float* d_x, const float* d_target,
+                                  const float* d_mask, int ncols, int nT, float lr,
+                                  double* loss_out, float* h_grad) {
+  if (!n || !d_x || !d_target || !d_mask) return net_fail(ASG_ERR_ARG, "null argument");
+  CKS_NET(check_batch(ncols, nT));
+  const size_t npos = (size_t)ncols * nT;
+  CKS_NET(net_ensure(n, npos));
+  cudaStream_t st = 0;
+  // the loss is a mean over the masked samples: their count, on the host
+  std::vector<float> hm(npos);
+  if (cudaMemcpy(hm.data(), d_mask, npos * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "mask download");
+  double ms = 0.0;
+  for (float v : hm) ms += v;
+  const float nmask = (float)(ms > 0.0 ? ms : 1.0);
+  cudaMemsetAsync(n->grad, 0, NPARAM * 4, st);
+  cudaMemsetAsync(n->loss, 0, sizeof(double), st);
+  CKS_NET(net_forward(n, d_x, n->yb, d_target, d_mask, 1.f / nmask, (int)npos, nT, true, st));
+  CKS_NET(net_backward(n, d_x, (int)npos, nT, st));
+  double l = 0.0;
+  if (cudaMemcpy(&l, n->loss, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "loss download");
+  if (loss_out) *loss_out = l / nmask;
+  if (h_grad && cudaMemcpy(h_grad, n->grad, NPARAM * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "gradient download");
+  if (lr > 0.f) {
+    n->adam_t++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f / (1.f - powf(b1, (float)n->adam_t));
+    const float c2 = 1.f / (1.f - powf(b2, (float)n->adam_t));
+    k_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(n->theta, n->adam_m, n->adam_v, n->grad, NPARAM,
+                                                  lr, b1, b2, c1, c2, 1e-8f);
+    CKS_NET(net_pack(n, st));
+  }
+  return cudaDeviceSynchronize() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "train step");
+}

@@ -142,3 +142,11 @@ int asg_launch_transpose(const float* in, float* out, int nz, int ncols, cudaStr
 int asg_roots_upload_t(const float2* w192, const float2* w64);
 int asg_roots_upload_xy(const float2* w192, const float2* w64);
 int asg_roots_upload_l2(const float2* w192, const float2* w64);
+
+// error reporting shared by the translation units (message for asg_last_error)
+int asg_fail_message(int code, const char* msg);
+#define CKS_NET(expr)            \
+  do {                           \
+    int s_ = (expr);             \
+    if (s_ != ASG_OK) return s_; \
+  } while (0)

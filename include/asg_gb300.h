@@ -230,6 +230,28 @@ int asg_flux_columns_device(const float* d_in, float* d_out, int ncols, int nT, 
                             double n_coef, double dz, double dt, double beta_tvd,
                             double cfl_target, int max_subcycles, void* stream);
 
+/* ---- learned KT corrector (no counterpart in the reference) ------------------
+ * A 1-D convolutional network along t (1 -> 64 -> 64 -> 64 -> 1 channels,
+ * kernel 5, GELU, zero padding per column) whose two 64x64 layers run as BF16
+ * tensor-core GEMMs with FP32 accumulation; FP32 master parameters, Adam.
+ * Batches are ncols device columns of nT samples (nT a multiple of 64). */
+typedef struct asg_net asg_net;
+int asg_net_param_count(void);   /* length of the FP32 parameter vector */
+int asg_net_create(asg_net** out);
+int asg_net_destroy(asg_net* net);
+/* Parameter vector layout: W1[64][5] b1[64] W2[64][64][5] b2[64] W3[64][64][5]
+ * b3[64] W4[64][5] b4[1] (W[out][in][tap]); setting resets the Adam state. */
+int asg_net_set_params(asg_net* net, const float* theta, int count);
+int asg_net_get_params(asg_net* net, float* theta, int count);
+/* y = net(x) on device buffers of ncols*nT floats, queued on `stream`. */
+int asg_net_forward(asg_net* net, const float* d_x, float* d_y, int ncols, int nT, void* stream);
+/* One step on a device batch: masked MSE loss of net(x) against target and its
+ * gradients (to h_grad, host, asg_net_param_count() floats, when not NULL);
+ * lr > 0 then applies an Adam update.  Synchronous. */
+int asg_net_train_step(asg_net* net, const float* d_x, const float* d_target,
+                       const float* d_mask, int ncols, int nT, float lr, double* loss_out,
+                       float* h_grad);
+
 /* Message of the last error on this thread. */
 const char* asg_last_error(void);
 
