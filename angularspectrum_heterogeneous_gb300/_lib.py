@@ -28,7 +28,8 @@ EXPORTED = [
     "asg_autotune", "asg_set_graphs", "asg_batch_create", "asg_batch_destroy",
     "asg_batch_set_graphs", "asg_batch_run", "asg_batch_last_run_ms",
     "asg_net_param_count", "asg_net_create", "asg_net_destroy", "asg_net_set_params",
-    "asg_net_get_params", "asg_net_forward", "asg_net_train_step",
+    "asg_net_get_params", "asg_net_forward", "asg_net_train_step", "asg_flux_columns_learned",
+    "asg_net_set_output_scale",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -125,6 +126,10 @@ def load(require_device: bool = True):
     lib.asg_net_get_params.argtypes = [P, F, C.c_int]
     lib.asg_net_forward.argtypes = [P, P, P, C.c_int, C.c_int, P]
     lib.asg_net_train_step.argtypes = [P, P, P, P, C.c_int, C.c_int, C.c_float, _DP, F]
+    lib.asg_net_set_output_scale.argtypes = [P, C.c_float]
+    lib.asg_flux_columns_learned.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double,
+                                             C.c_double, C.c_double, C.c_double, C.c_int,
+                                             C.c_int, C.c_float, C.POINTER(C.c_int), P]
     lib.asg_batch_create.argtypes = [C.POINTER(P), C.c_int, C.POINTER(P)]
     lib.asg_batch_destroy.argtypes = [P]
     lib.asg_batch_set_graphs.argtypes = [P, C.c_int]

@@ -421,6 +421,7 @@ struct asg_net {
   bf16_t *wg2 = nullptr, *wt2 = nullptr, *wg3 = nullptr, *wt3 = nullptr;
   double* loss = nullptr;
   int adam_t = 0;
+  float gamma = 1.f;  // output scale of the learned step (see GateParams)
   // activations of the largest batch seen
   size_t cap = 0;
   float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *dy = nullptr, *yb = nullptr;
@@ -617,4 +618,176 @@ extern "C" int asg_net_train_step(asg_net* n, const float* d_x, const float* d_t
     CKS_NET(net_pack(n, st));
   }
   return cudaDeviceSynchronize() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "train step");
+}
+
+// ---------------------------------------------------------------------------
+// Learned KT step on columns.
+//
+// Gate (one warp per column, the column in a skewed shared-memory copy):
+//   s      = max|u|,  steep = max_t |u[t+1] - u[t]|
+//   n_sub  = the per-column sub-cycle count of the plain KT step at cfl_target
+//   learned when n_sub >= min_sub and steep <= shock_ratio * s: one coarse KT
+//     step of the full dz, written to out and, in CFL units, to the network's
+//     input rows (compacted, in the order the columns claim them);
+//   otherwise the plain sub-cycled KT step (the fallback) is written to out.
+// Apply: out[c][t] += s gamma cfl^3 y[k][t] for the learned columns,
+// t = 1 .. nT-2 (the KT step never changes the end samples).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct GateParams {
+  const float* in;
+  float* out;
+  int ncols, nT;
+  float ndt, dz, cfl_target;
+  int max_sub, min_sub, mc;
+  float shock_ratio;
+  // The network sees the coarse column in CFL units (w = u ndt dz, divided by
+  // CFL_IN), so that the column's CFL number is visible to it, and predicts
+  // the correction in units of s gamma cfl^3 (cfl = ndt s dz): the difference
+  // between one SSP-RK2 KT step and the sub-cycled step is third order in the
+  // column's CFL number, so these targets are of order one at every peak.
+  float gamma;
+  float in_scale;     // ndt dz / CFL_IN
+  float* xrows;       // [ncols][nT] compacted network input
+  int* list_col;      // [ncols]
+  float* list_s;      // [ncols] output scale of each learned column
+  int* counter;       // learned columns so far (starts at zero)
+};
+
+template <int CH>
+__global__ void __launch_bounds__(256) k_flux_gate(GateParams p) {
+  extern __shared__ float sk_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + warp;
+  if (c >= p.ncols) return;
+  const int nT = p.nT;
+  const unsigned mask = 0xffffffffu;
+  SkewColumn col{sk_raw + warp * skew_floats(32 * CH)};
+  const float* src = p.in + (size_t)c * nT;
+  float s = 0.f, steep = 0.f;
+  for (int t = lane; t < nT; t += 32) {
+    const float u = src[t];
+    col.set(t, u);
+    s = fmaxf(s, fabsf(u));
+    if (t + 1 < nT) steep = fmaxf(steep, fabsf(src[t + 1] - u));
+  }
+  s = warp_max(s);
+  steep = warp_max(steep);
+  __syncwarp(mask);
+  int nsub = 1;
+  if (p.cfl_target > 0.f) {
+    const float cfl = p.ndt * s * p.dz;
+    if (!(cfl <= p.cfl_target || s < 1e-30f)) {
+      const float q = ceilf(cfl / p.cfl_target);
+      nsub = (q > (float)p.max_sub) ? p.max_sub : (int)q;
+    }
+  }
+  const bool learned = nsub >= p.min_sub && steep <= p.shock_ratio * s && s > 1e-30f;
+  const int steps = learned ? 1 : nsub;
+  const float dzs = p.dz / (float)steps;
+  for (int k = 0; k < steps; ++k) {
+    if (p.mc) kt_column_step_chunk<CH, true>(col, nT, p.ndt, dzs, mask);
+    else kt_column_step_chunk<CH, false>(col, nT, p.ndt, dzs, mask);
+  }
+  float* dst = p.out + (size_t)c * nT;
+  for (int t = lane; t < nT; t += 32) dst[t] = col.get(t);
+  if (learned) {
+    int k = 0;
+    if (lane == 0) {
+      k = atomicAdd(p.counter, 1);
+      const float cfl = p.ndt * s * p.dz;
+      p.list_col[k] = c;
+      p.list_s[k] = s * p.gamma * cfl * cfl * cfl;
+    }
+    k = __shfl_sync(mask, k, 0);
+    float* xr = p.xrows + (size_t)k * nT;
+    for (int t = lane; t < nT; t += 32) xr[t] = col.get(t) * p.in_scale;
+  }
+}
+
+__global__ void k_apply_correction(const float* __restrict__ y, const int* __restrict__ list_col,
+                                   const float* __restrict__ list_s, const int* __restrict__ counter,
+                                   float* __restrict__ out, int nT) {
+  const int k = blockIdx.x;
+  if (k >= *counter) return;
+  const int c = list_col[k];
+  const float s = list_s[k];
+  for (int t = threadIdx.x; t < nT; t += blockDim.x)
+    if (t >= 1 && t < nT - 1) out[(size_t)c * nT + t] += s * y[(size_t)k * nT + t];
+}
+
+template <int CH>
+int launch_gate(const GateParams& p, cudaStream_t st) {
+  const size_t smem = (size_t)8 * skew_floats(32 * CH) * sizeof(float);
+  k_flux_gate<CH><<<(p.ncols + 7) / 8, 256, smem, st>>>(p);
+  return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
+}  // namespace
+
+// Scale of the network's output in the learned step (see GateParams::gamma).
+extern "C" int asg_net_set_output_scale(asg_net* n, float gamma) {
+  if (!n || !(gamma > 0.f)) return net_fail(ASG_ERR_ARG, "bad output scale");
+  n->gamma = gamma;
+  return ASG_OK;
+}
+
+// Learned KT step on device columns (see the gate above).  n_coef = N (the
+// nonlinearity coefficient); the network input rows and the column list live
+// in the net's own activation buffers (grown as needed).  Synchronous:
+// *n_learned receives the number of columns that took the learned path.
+extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_out, int ncols,
+                                        int nT, int flux, double n_coef, double dz, double dt,
+                                        double cfl_target, int max_subcycles, int min_subcycles,
+                                        float shock_ratio, int* n_learned, void* stream) {
+  if (!n || !d_in || !d_out || d_in == d_out) return net_fail(ASG_ERR_ARG, "bad argument");
+  if (flux != ASG_FLUX_KT && flux != ASG_FLUX_KT_MINMOD)
+    return net_fail(ASG_ERR_ARG, "the learned step corrects the KT schemes only");
+  CKS_NET(check_batch(ncols, nT));
+  if (nT > 1024) return net_fail(ASG_ERR_SHAPE, "learned step: columns up to 1024 samples");
+  const size_t npos = (size_t)ncols * nT;
+  CKS_NET(net_ensure(n, npos));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // input rows in z1 (npos * 64 floats), the column list and scales in z2,
+  // the counter in the loss slot
+  float* xrows = n->z1;
+  int* list_col = reinterpret_cast<int*>(n->z2);
+  float* list_s = n->z2 + ncols;
+  int* counter = reinterpret_cast<int*>(n->loss);
+  if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "counter reset");
+  GateParams g;
+  g.in = d_in;
+  g.out = d_out;
+  g.ncols = ncols;
+  g.nT = nT;
+  g.ndt = (float)(n_coef / dt);
+  g.dz = (float)dz;
+  g.cfl_target = (float)cfl_target;
+  g.max_sub = max_subcycles > 0 ? max_subcycles : 1024;
+  g.min_sub = min_subcycles;
+  g.mc = flux == ASG_FLUX_KT;
+  g.shock_ratio = shock_ratio;
+  g.gamma = n->gamma;
+  g.in_scale = (float)(n_coef / dt * dz / 0.3);  // CFL_IN = 0.3
+  g.xrows = xrows;
+  g.list_col = list_col;
+  g.list_s = list_s;
+  g.counter = counter;
+  const int ch = (nT + 31) / 32;
+  const int s = ch <= 2 ? launch_gate<2>(g, st) : ch <= 4 ? launch_gate<4>(g, st)
+              : ch <= 8 ? launch_gate<8>(g, st) : ch <= 16 ? launch_gate<16>(g, st)
+              : launch_gate<32>(g, st);
+  if (s != ASG_OK) return net_fail(s, "gate launch");
+  int k = 0;
+  if (cudaMemcpyAsync(&k, counter, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "learned-column count");
+  if (n_learned) *n_learned = k;
+  if (k == 0) return ASG_OK;
+  CKS_NET(net_forward(n, xrows, n->yb, nullptr, nullptr, 0.f, k * nT, nT, false, st));
+  k_apply_correction<<<k, 256, 0, st>>>(n->yb, list_col, list_s, counter, d_out, nT);
+  if (cudaPeekAtLastError() != cudaSuccess) return net_fail(ASG_ERR_CUDA, "apply launch");
+  return cudaStreamSynchronize(st) == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "learned step");
 }

@@ -252,6 +252,23 @@ int asg_net_train_step(asg_net* net, const float* d_x, const float* d_target,
                        const float* d_mask, int ncols, int nT, float lr, double* loss_out,
                        float* h_grad);
 
+/* Output scale gamma of the learned step (fitted on the training data):
+ * out = coarse + s * gamma * cfl^3 * net(coarse * n_coef/dt * dz / 0.3),
+ * s = max|u| of the column, cfl = n_coef/dt * s * dz its CFL number. */
+int asg_net_set_output_scale(asg_net* net, float gamma);
+
+/* Learned KT step on device columns (in -> out, ncols x nT floats, nT a
+ * multiple of 64 up to 1024; in != out).  Per column: s = max|u|, the plain
+ * KT sub-cycle count n_sub at cfl_target, and the steepness max|u[t+1]-u[t]|.
+ * When n_sub >= min_subcycles and the steepness is at most shock_ratio * s,
+ * one coarse KT step of the full dz plus the scaled correction above; otherwise
+ * the plain sub-cycled KT step (the fallback).  Synchronous; *n_learned
+ * receives the number of corrected columns. */
+int asg_flux_columns_learned(asg_net* net, const float* d_in, float* d_out, int ncols, int nT,
+                             int flux, double n_coef, double dz, double dt, double cfl_target,
+                             int max_subcycles, int min_subcycles, float shock_ratio,
+                             int* n_learned, void* stream);
+
 /* Message of the last error on this thread. */
 const char* asg_last_error(void);
 
