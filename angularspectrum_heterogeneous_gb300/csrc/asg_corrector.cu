@@ -424,6 +424,12 @@ struct asg_net {
   float gamma = 1.f;  // output scale of the learned step (see GateParams)
   // activations of the largest batch seen
   size_t cap = 0;
+  // inference of the learned step: input rows of every learned column, the
+  // column list, and activations for one chunk of rows at a time
+  size_t inf_cols = 0, inf_pos = 0;
+  float *inf_x = nullptr, *inf_s = nullptr, *inf_y = nullptr;
+  int* inf_col = nullptr;
+  bf16_t *inf_a = nullptr, *inf_b = nullptr;
   float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *dy = nullptr, *yb = nullptr;
   bf16_t *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *d1 = nullptr, *d2 = nullptr;
   int nsm = 152;
@@ -437,6 +443,38 @@ static void net_free_acts(asg_net* n) {
   n->z1 = n->z2 = n->z3 = n->dy = n->yb = nullptr;
   n->h1 = n->h2 = n->h3 = n->d1 = n->d2 = nullptr;
   n->cap = 0;
+}
+
+static void net_free_inf(asg_net* n) {
+  void* ps[] = {n->inf_x, n->inf_s, n->inf_y, n->inf_col, n->inf_a, n->inf_b};
+  for (void* p : ps) cudaFree(p);
+  n->inf_x = n->inf_s = n->inf_y = nullptr;
+  n->inf_col = nullptr;
+  n->inf_a = n->inf_b = nullptr;
+  n->inf_cols = n->inf_pos = 0;
+}
+
+// positions of one inference chunk: two BF16 activation buffers of 1 GiB
+constexpr size_t INF_CHUNK_POS = (size_t)1 << 23;
+
+static int net_ensure_inf(asg_net* n, size_t ncols, int nT) {
+  const size_t npos = ncols * (size_t)nT;
+  if (n->inf_cols >= ncols && n->inf_pos >= npos) return ASG_OK;
+  net_free_inf(n);
+  const size_t chunk = npos < INF_CHUNK_POS ? npos : INF_CHUNK_POS;
+  bool ok = cudaMalloc(&n->inf_x, npos * 4) == cudaSuccess &&
+            cudaMalloc(&n->inf_s, ncols * 4) == cudaSuccess &&
+            cudaMalloc(&n->inf_col, (ncols + 1) * 4) == cudaSuccess &&
+            cudaMalloc(&n->inf_y, chunk * 4) == cudaSuccess &&
+            cudaMalloc(&n->inf_a, chunk * NCH * 2) == cudaSuccess &&
+            cudaMalloc(&n->inf_b, chunk * NCH * 2) == cudaSuccess;
+  if (!ok) {
+    net_free_inf(n);
+    return net_fail(ASG_ERR_NOMEM, "learned step scratch: cudaMalloc failed");
+  }
+  n->inf_cols = ncols;
+  n->inf_pos = npos;
+  return ASG_OK;
 }
 
 static int net_ensure(asg_net* n, size_t npos) {
@@ -509,6 +547,22 @@ static int net_backward(asg_net* n, const float* x, int npos, int nT, cudaStream
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "backward launch");
 }
 
+// inference: x [npos] -> y [npos] with two BF16 activation buffers
+static int net_infer(asg_net* n, const float* x, float* y, int npos, int nT, bf16_t* a,
+                     bf16_t* b, cudaStream_t st) {
+  CKS_NET(conv_smem_attr());
+  const int tiles = npos / TP;
+  const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
+  k_layer1_fwd<<<4 * n->nsm, 256, 0, st>>>(x, n->theta, nullptr, a, npos, nT);
+  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(a, n->wg2, n->theta + OFF_B2, nullptr, nullptr, b,
+                                             npos, nT);
+  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(b, n->wg3, n->theta + OFF_B3, nullptr, nullptr, a,
+                                             npos, nT);
+  k_layer4_fwd<<<4 * n->nsm, 256, 0, st>>>(a, n->theta, y, nullptr, nullptr, 0.f, nullptr,
+                                           nullptr, npos, nT);
+  return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "inference launch");
+}
+
 extern "C" int asg_net_param_count(void) { return NPARAM; }
 
 extern "C" int asg_net_create(asg_net** out) {
@@ -541,6 +595,7 @@ extern "C" int asg_net_create(asg_net** out) {
 extern "C" int asg_net_destroy(asg_net* n) {
   if (!n) return ASG_OK;
   net_free_acts(n);
+  net_free_inf(n);
   void* ps[] = {n->theta, n->adam_m, n->adam_v, n->grad, n->wg2, n->wt2, n->wg3, n->wt3, n->loss};
   for (void* p : ps) cudaFree(p);
   delete n;
@@ -574,10 +629,15 @@ extern "C" int asg_net_forward(asg_net* n, const float* d_x, float* d_y, int nco
                                void* stream) {
   if (!n || !d_x || !d_y) return net_fail(ASG_ERR_ARG, "null argument");
   CKS_NET(check_batch(ncols, nT));
-  const size_t npos = (size_t)ncols * nT;
-  CKS_NET(net_ensure(n, npos));
-  return net_forward(n, d_x, d_y, nullptr, nullptr, 0.f, (int)npos, nT, false,
-                     static_cast<cudaStream_t>(stream));
+  CKS_NET(net_ensure_inf(n, (size_t)ncols, nT));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int rows_per_chunk = (int)(INF_CHUNK_POS / (size_t)nT);
+  for (int r0 = 0; r0 < ncols; r0 += rows_per_chunk) {
+    const int rows = ncols - r0 < rows_per_chunk ? ncols - r0 : rows_per_chunk;
+    CKS_NET(net_infer(n, d_x + (size_t)r0 * nT, d_y + (size_t)r0 * nT, rows * nT, nT, n->inf_a,
+                      n->inf_b, st));
+  }
+  return ASG_OK;
 }
 
 // One training step on a device batch: loss (masked MSE) and gradients; with
@@ -706,15 +766,16 @@ __global__ void __launch_bounds__(256) k_flux_gate(GateParams p) {
   }
 }
 
+// rows row0 .. row0 + gridDim.x - 1 of the learned list; y holds their outputs
 __global__ void k_apply_correction(const float* __restrict__ y, const int* __restrict__ list_col,
-                                   const float* __restrict__ list_s, const int* __restrict__ counter,
+                                   const float* __restrict__ list_s, int row0,
                                    float* __restrict__ out, int nT) {
-  const int k = blockIdx.x;
-  if (k >= *counter) return;
+  const int k = row0 + blockIdx.x;
   const int c = list_col[k];
   const float s = list_s[k];
+  const float* yr = y + (size_t)blockIdx.x * nT;
   for (int t = threadIdx.x; t < nT; t += blockDim.x)
-    if (t >= 1 && t < nT - 1) out[(size_t)c * nT + t] += s * y[(size_t)k * nT + t];
+    if (t >= 1 && t < nT - 1) out[(size_t)c * nT + t] += s * yr[t];
 }
 
 template <int CH>
@@ -734,8 +795,9 @@ extern "C" int asg_net_set_output_scale(asg_net* n, float gamma) {
 }
 
 // Learned KT step on device columns (see the gate above).  n_coef = N (the
-// nonlinearity coefficient); the network input rows and the column list live
-// in the net's own activation buffers (grown as needed).  Synchronous:
+// nonlinearity coefficient); the network input rows, the column list and the
+// activations of one chunk of rows are the net's own scratch (grown as
+// needed, activations bounded by the chunk).  Synchronous:
 // *n_learned receives the number of columns that took the learned path.
 extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_out, int ncols,
                                         int nT, int flux, double n_coef, double dz, double dt,
@@ -746,15 +808,12 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
     return net_fail(ASG_ERR_ARG, "the learned step corrects the KT schemes only");
   CKS_NET(check_batch(ncols, nT));
   if (nT > 1024) return net_fail(ASG_ERR_SHAPE, "learned step: columns up to 1024 samples");
-  const size_t npos = (size_t)ncols * nT;
-  CKS_NET(net_ensure(n, npos));
+  CKS_NET(net_ensure_inf(n, (size_t)ncols, nT));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // input rows in z1 (npos * 64 floats), the column list and scales in z2,
-  // the counter in the loss slot
-  float* xrows = n->z1;
-  int* list_col = reinterpret_cast<int*>(n->z2);
-  float* list_s = n->z2 + ncols;
-  int* counter = reinterpret_cast<int*>(n->loss);
+  float* xrows = n->inf_x;
+  int* list_col = n->inf_col;
+  float* list_s = n->inf_s;
+  int* counter = n->inf_col + ncols;
   if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "counter reset");
   GateParams g;
@@ -785,9 +844,12 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
       cudaStreamSynchronize(st) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "learned-column count");
   if (n_learned) *n_learned = k;
-  if (k == 0) return ASG_OK;
-  CKS_NET(net_forward(n, xrows, n->yb, nullptr, nullptr, 0.f, k * nT, nT, false, st));
-  k_apply_correction<<<k, 256, 0, st>>>(n->yb, list_col, list_s, counter, d_out, nT);
-  if (cudaPeekAtLastError() != cudaSuccess) return net_fail(ASG_ERR_CUDA, "apply launch");
+  const int rows_per_chunk = (int)(INF_CHUNK_POS / (size_t)nT);
+  for (int r0 = 0; r0 < k; r0 += rows_per_chunk) {
+    const int rows = k - r0 < rows_per_chunk ? k - r0 : rows_per_chunk;
+    CKS_NET(net_infer(n, xrows + (size_t)r0 * nT, n->inf_y, rows * nT, nT, n->inf_a, n->inf_b, st));
+    k_apply_correction<<<rows, 256, 0, st>>>(n->inf_y, list_col, list_s, r0, d_out, nT);
+    if (cudaPeekAtLastError() != cudaSuccess) return net_fail(ASG_ERR_CUDA, "apply launch");
+  }
   return cudaStreamSynchronize(st) == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "learned step");
 }

@@ -381,6 +381,91 @@ def run_batch_arm(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# Learned KT step on the workload's columns
+# ---------------------------------------------------------------------------
+LEARN_DZ, LEARN_CFL, LEARN_MIN_SUB = 2e-3, 0.01, 10
+NET_FLOP_PER_SAMPLE = 2 * 5 * (1 * 64 + 64 * 64 + 64 * 64 + 64 * 1)  # 83,200
+
+
+def run_learned_arm(args):
+    """The Burgers stage of the workload (all 262 k columns of 1024 samples of
+    the 512x512x1024 piston field, a 2 mm KT step): the plain KT step
+    sub-cycled at CFL 0.01 against the learned step (one coarse step + the
+    network on columns needing >= 10 sub-cycles, plain fallback elsewhere).
+    The network is trained first on columns of seeded focused fields."""
+    import torch
+    from angularspectrum_heterogeneous_gb300 import corrector as CR
+    torch.cuda.set_device(0)
+    n_coef = 3.5 / (2 * 1540.0 ** 3 * 1000.0)
+    dt = 1e-8
+    t0 = time.time()
+    pool = CR.focused_field_columns(6, grid=(64, 64, 1024), steps=20, seed=1)
+    net = CR.Corrector(CR.init_params(0))
+    hist = CR.train(net, pool, n_coef, LEARN_DZ, dt, LEARN_CFL, steps=1000, batch=256, lr=3e-3)
+    t_train = time.time() - t0
+    cols = torch.from_numpy(workload_field().reshape(-1, NT)).cuda()
+    out = torch.empty_like(cols)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, r
+
+    reps = max(1, args.steps)
+    ms_plain, _ = timed(lambda: CR._flux_device(cols, out, n_coef, LEARN_DZ, dt, LEARN_CFL, 4096), reps)
+    plain = out.clone()
+    ms_coarse, _ = timed(lambda: CR._flux_device(cols, out, n_coef, LEARN_DZ, dt, 0.0, 1), reps)
+    coarse = out.clone()
+    ms_learned, nl = timed(lambda: CR.learned_flux(net, cols, n_coef, LEARN_DZ, dt, LEARN_CFL,
+                                                   LEARN_MIN_SUB, out=out)[1], reps)
+    learned = out.clone()
+    # the network alone on the learned columns' share
+    xr = torch.randn(max(nl, 1), NT, device="cuda")
+    ms_net, _ = timed(lambda: net.forward(xr), reps)
+
+    def rel(a, b):
+        return float(((a - b) ** 2).sum().sqrt() / (b ** 2).sum().sqrt())
+
+    s = cols.abs().amax(1)
+    sel = torch.ceil(n_coef / dt * s * LEARN_DZ / LEARN_CFL) >= LEARN_MIN_SUB
+    vox = cols.numel()
+    peak_tf = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_tf = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        pass
+    net_tf = max(nl, 1) * NT * NET_FLOP_PER_SAMPLE / (ms_net / 1e3) / 1e12
+    line = {"metric": "voxel-steps/s", "value": vox / (ms_learned / 1e3), "unit": "voxel-steps/s",
+            "n_gpus": 1, "steps": reps, "warmup": 1, "ms_per_step": ms_learned,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
+            "data": "synthetic",
+            "config": {"workload": "Burgers stage of the 512x512x1024 2 MPa piston field, 2 mm "
+                                   "KT step; learned (coarse + network where >= 10 sub-cycles) vs "
+                                   "plain KT sub-cycled at CFL 0.01 (configs[4] shape)",
+                       "columns": int(cols.shape[0]), "learned_columns": int(nl),
+                       "train_steps": len(hist), "train_seconds": t_train,
+                       "final_loss": float(np.mean(hist[-20:]))},
+            "plain_kt": {"value": vox / (ms_plain / 1e3), "ms": ms_plain},
+            "coarse_kt": {"value": vox / (ms_coarse / 1e3), "ms": ms_coarse},
+            "speedup_vs_plain": ms_plain / ms_learned,
+            "rel_l2_vs_plain": {"learned": rel(learned, plain), "coarse": rel(coarse, plain),
+                                "learned_columns_only": rel(learned[sel], plain[sel]),
+                                "coarse_learned_columns_only": rel(coarse[sel], plain[sel])},
+            "network": {"ms": ms_net, "tflops": net_tf,
+                        "frac_of_bf16_peak": (net_tf / peak_tf) if peak_tf else None,
+                        "flop_per_sample": NET_FLOP_PER_SAMPLE}}
+    net.close()
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -392,13 +477,17 @@ def main():
                     help="profiling only: a smaller grid with the same options")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"],
-                    help="batch: the 64-instance batched march (not the headline line)")
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "learned"],
+                    help="batch: the 64-instance batched march; learned: the learned KT "
+                         "step against the plain one (neither is the headline line)")
     args = ap.parse_args()
     if args.grid:
         set_grid(*args.grid)
     if args.workload == "batch" and args.impl != "reference":
         run_batch_arm(args)
+        return
+    if args.workload == "learned" and args.impl != "reference":
+        run_learned_arm(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)
