@@ -109,11 +109,17 @@ ASG_DEV float minmod3(float a, float b, float c) {
   bool ok = (a * b > 0.f) && (b * c > 0.f);
   return ok ? sgnf(a) * fminf(fminf(fabsf(a), fabsf(b)), fabsf(c)) : 0.f;
 }
-// limited slope at a cell given its left/right neighbours (MC or minmod)
+// limited slope at a cell given its left/right neighbours (MC or minmod).
+// MC: minmod3(2 dm, (dm + dp)/2, 2 dp) = sign(dm) 2 min(|dm|, |dm + dp|/4, |dp|)
+// when dm dp > 0 (then all three arguments share the sign), else 0; the
+// power-of-two scalings are exact, so this is the same number with fewer
+// operations.
 template <bool MC>
 ASG_DEV float kt_slope(float um1, float u0, float up1) {
-  float dm = u0 - um1, dp = up1 - u0;
-  return MC ? minmod3(2.f * dm, 0.5f * (dm + dp), 2.f * dp) : minmod2(dm, dp);
+  const float dm = u0 - um1, dp = up1 - u0;
+  const float m = MC ? 2.f * fminf(fminf(fabsf(dm), fabsf(dp)), 0.25f * fabsf(dm + dp))
+                     : fminf(fabsf(dm), fabsf(dp));
+  return (dm * dp > 0.f) ? copysignf(m, dm) : 0.f;
 }
 // KT interface flux from the reconstructed states (:772-793)
 ASG_DEV float kt_fh(float um, float up) {
@@ -256,11 +262,72 @@ ASG_DEV void load_window4(const Col& col, int t0, int nT, float (&w)[CH + 4]) {
   }
 }
 
+// Column length exactly 32 CH: only the first lane's two leading and the last
+// lane's two trailing window values lie outside the column, and only their
+// slopes and end-sample rhs need zeroing, so the per-point range tests go.
+template <int CH, class Col>
+ASG_DEV void load_window4_exact(const Col& col, int t0, int lane, float (&w)[CH + 4]) {
+  const bool first = lane != 0, last = lane != 31;
+  w[0] = first ? col.get(t0 > 2 ? t0 - 2 : 0) : 0.f;
+  w[1] = first ? col.get(t0 > 1 ? t0 - 1 : 0) : 0.f;
+#pragma unroll
+  for (int i = 2; i < CH + 2; ++i) w[i] = col.get(t0 - 2 + i);
+  w[CH + 2] = last ? col.get(last ? t0 + CH : t0) : 0.f;
+  w[CH + 3] = last ? col.get(last ? t0 + CH + 1 : t0) : 0.f;
+}
+
+// One stage of the exact-length KT step, streamed along the lane's window:
+// slopes, interface fluxes and the update are formed point by point (only
+// the previous slope and flux stay live), and each updated value is written
+// as soon as it is known (every lane has its window in registers by then):
+//   stage 1: col[t] = u[t] + dz rhs(w)
+//   stage 2: col[t] = u[t]/2 + (w[t] + dz rhs(w))/2
+template <int CH, bool MC, bool STAGE2, class Col>
+ASG_DEV void kt_stage_exact(const Col& col, const float (&w)[CH + 4], const float (&u)[CH],
+                            int t0, int lane, float ndt, float dz) {
+  const bool first = lane != 0, last = lane != 31;
+  // slope at window position i+1 (t = t0 - 1 + i); zero at the column ends
+  auto slope = [&](int i) {
+    const float v = kt_slope<MC>(w[i], w[i + 1], w[i + 2]);
+    if (i <= 1) return first ? v : 0.f;
+    if (i >= CH) return last ? v : 0.f;
+    return v;
+  };
+  float sl = slope(0), sr = slope(1);
+  float fprev = kt_fh(w[1] + 0.5f * sl, w[2] - 0.5f * sr);  // interface t0 - 1/2
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    sl = sr;
+    sr = slope(i + 2);
+    const float f = kt_fh(w[i + 2] + 0.5f * sl, w[i + 3] - 0.5f * sr);  // t0 + i + 1/2
+    float rhs = -ndt * (f - fprev);
+    if (i == 0) rhs = first ? rhs : 0.f;
+    if (i == CH - 1) rhs = last ? rhs : 0.f;
+    fprev = f;
+    if (STAGE2) col.set(t0 + i, 0.5f * u[i] + 0.5f * (w[i + 2] + dz * rhs));
+    else col.set(t0 + i, u[i] + dz * rhs);
+  }
+}
+
 // one SSP-RK2 KT step of size dz on the column
 template <int CH, bool MC, class Col>
 ASG_DEV void kt_column_step_chunk(const Col& col, int nT, float ndt, float dz, unsigned mask) {
   const int lane = threadIdx.x & 31;
   const int t0 = lane * CH;
+  if (nT == 32 * CH && CH >= 2) {  // uniform across the warp
+    float w[CH + 4], u[CH];
+    load_window4_exact<CH>(col, t0, lane, w);
+#pragma unroll
+    for (int i = 0; i < CH; ++i) u[i] = w[i + 2];
+    __syncwarp(mask);  // every window is read before any lane writes
+    kt_stage_exact<CH, MC, false>(col, w, u, t0, lane, ndt, dz);
+    __syncwarp(mask);
+    load_window4_exact<CH>(col, t0, lane, w);
+    __syncwarp(mask);
+    kt_stage_exact<CH, MC, true>(col, w, u, t0, lane, ndt, dz);
+    __syncwarp(mask);
+    return;
+  }
   float w[CH + 4];
   load_window4<CH, MC>(col, t0, nT, w);
   float u[CH], rhs[CH];

@@ -38,7 +38,7 @@ enum TMode : int { TM_PLAIN = 0, TM_FLUX = 1, TM_STATS = 2 };
 // (2 blocks per SM); the other modes run 3 blocks per SM with 16 columns or
 // from 512 samples up (shared memory allows no more) and 4 otherwise.
 template <class PL, int MODE, int C>
-__global__ void __launch_bounds__(256, (MODE == 1 ? 2 : ((PL::N >= 512 || C == 16) ? 3 : 4)))
+__global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 : 2) : ((PL::N >= 512 || C == 16) ? 3 : 4)))
     tk_fast(TParams p) {
   if (*p.status != 0) return;
   static_assert(C == 8 || C == 16, "8 or 16 columns per block");
