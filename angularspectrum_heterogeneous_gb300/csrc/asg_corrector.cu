@@ -1,7 +1,7 @@
 // Learned KT corrector: a 1-D convolutional network along t that corrects one
 // coarse KT step of a column towards the fully sub-cycled KT step.
 //
-//   h1 = GELU(conv(x,  W1[64,1,5])  + b1)      CUDA cores
+//   h1 = GELU(conv(x,  W1[64,1,5])  + b1)      CUDA cores (GELU in its tanh form)
 //   h2 = GELU(conv(h1, W2[64,64,5]) + b2)      BF16 tensor cores, FP32 accumulation
 //   h3 = GELU(conv(h2, W3[64,64,5]) + b3)      BF16 tensor cores, FP32 accumulation
 //   y  =      conv(h3, W4[1,64,5])  + b4       CUDA cores
@@ -11,7 +11,7 @@
 // _kt_flux_adaptive, angular_spectrum_solver.py:833-859) produces the
 // training targets through the column kernels of this library.
 //
-// Data layout: a batch of ncols columns of nT samples (nT % 64 == 0), position
+// Data layout: a batch of ncols columns of nT samples (nT % 128 == 0), position
 // pos = column * nT + t.  Activations are position-major [pos][64 channels]
 // (BF16, 128 B per position); pre-activations z are kept in FP32 for the
 // backward pass.  Parameters live in one FP32 vector theta (layout below);
@@ -53,9 +53,22 @@ __device__ __forceinline__ bf16_t f2bf(float f) {
 }
 __device__ __forceinline__ float bf2f(bf16_t h) { return __uint_as_float(((unsigned)h) << 16); }
 
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))), with
+// the hardware tanh (relative error ~2^-11, below the BF16 rounding of the
+// activations); the derivative uses the same tanh value.
+__device__ __forceinline__ float tanh_hw(float u) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+__device__ __forceinline__ float gelu_f(float z) {
+  const float t = tanh_hw(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
+  return 0.5f * z * (1.f + t);
+}
 __device__ __forceinline__ float gelu_grad_f(float z) {
-  return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * expf(-0.5f * z * z) * 0.39894228040143268f;
+  const float t = tanh_hw(0.7978845608028654f * fmaf(0.044715f * z * z, z, z));
+  return 0.5f * (1.f + t) +
+         0.5f * z * (1.f - t * t) * 0.7978845608028654f * fmaf(0.134145f, z * z, 1.f);
 }
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1, unsigned a2,
@@ -75,80 +88,145 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], unsigned a0, unsigned a1
 // A block of 4 warps owns 64 positions x 64 channels per tile (persistent over
 // tiles); warp w computes positions w*16 .. w*16+15 for all 64 channels.
 // ---------------------------------------------------------------------------
-constexpr int WS = KDIM + 8;   // row stride of the weight tile (bf16): conflict-free fragments
+constexpr int WS = KDIM + 8;   // row stride of the weight tile (bf16): conflict-free ldmatrix rows
 constexpr int XS = NCH + 8;    // row stride of the activation tile
-constexpr int TP = 64;         // positions per tile
-constexpr size_t CONV_SMEM = (size_t)(NCH * WS + (TP + 4) * XS) * sizeof(bf16_t);
+constexpr int TP = 64;         // positions per chunk of the weight-gradient kernel
+constexpr int TPC = 128;       // positions per tile of the convolution kernel
+constexpr size_t CONV_SMEM =
+    (size_t)(NCH * WS + (TPC + 4) * XS) * sizeof(bf16_t) + (TPC + 8) * sizeof(float);
 
-template <int MODE>
-__global__ void __launch_bounds__(128) k_conv64(const bf16_t* __restrict__ X,
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+// A block of 4 warps owns 128 positions x 64 channels per tile (persistent
+// over tiles); warp w computes positions w*32 .. w*32+31 (4 n-tiles) for all
+// 64 channels (4 m-tiles): per k-step of 16, four ldmatrix.x4 for the weight
+// fragments, two for the activation fragments, sixteen MMAs.
+// FUSE_L1 (inference): X is the FP32 network input x; the staged rows are the
+// first layer's output h1 = GELU(b1 + conv(x, W1)), computed in place of a
+// load (zero outside the column), so h1 never goes to memory.
+template <int MODE, bool FUSE_L1 = false>
+__global__ void __launch_bounds__(128) k_conv64(const void* __restrict__ Xv,
                                                 const bf16_t* __restrict__ Wg,
                                                 const float* __restrict__ bias,
                                                 const float* __restrict__ Zin,
                                                 float* __restrict__ Zout,
-                                                bf16_t* __restrict__ H, int npos, int nT) {
+                                                bf16_t* __restrict__ H, int npos, int nT,
+                                                const float* __restrict__ th = nullptr) {
   extern __shared__ uint4 smem_u4[];
   bf16_t* Ws = reinterpret_cast<bf16_t*>(smem_u4);
-  bf16_t* Xs = Ws + NCH * WS;
+  bf16_t* Xs = Ws + NCH * WS;  // input rows pos0-2 .. pos0+TPC+1; reused for the output tile
+  float* xs = reinterpret_cast<float*>(Xs + (TPC + 4) * XS);  // FUSE_L1: x[pos0-4 .. pos0+TPC+3]
+  const bf16_t* X = static_cast<const bf16_t*>(Xv);
+  const float* xin = static_cast<const float*>(Xv);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int gid = lane >> 2, tig = lane & 3;
+  const int lm = lane >> 3, lr = lane & 7;  // ldmatrix: matrix and row this lane addresses
+  float w1[KT5], b1 = 0.f;  // FUSE_L1: the first layer's weights of channel tid % 64
+  if (FUSE_L1) {
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) w1[j] = th[OFF_W1 + (tid & 63) * KT5 + j];
+    b1 = th[OFF_B1 + (tid & 63)];
+  }
   // weights once per block: 64 rows of 320 bf16 = 40 uint4 each
   for (int i = tid; i < NCH * (KDIM / 8); i += blockDim.x) {
     const int o = i / (KDIM / 8), c = i - o * (KDIM / 8);
     *reinterpret_cast<uint4*>(Ws + o * WS + c * 8) =
         *reinterpret_cast<const uint4*>(Wg + (size_t)o * KDIM + c * 8);
   }
-  const int ntiles = npos / TP;
+  const int ntiles = npos / TPC;
+  const int nb = warp * 32;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int pos0 = tile * TP;
+    const int pos0 = tile * TPC;
     const int cbeg = (pos0 / nT) * nT, cend = cbeg + nT;
     __syncthreads();  // previous tile's readers are done (and the weights are in)
-    for (int i = tid; i < (TP + 4) * (NCH / 8); i += blockDim.x) {
-      const int r = i / (NCH / 8), c = i - r * (NCH / 8);
-      const int pos = pos0 - 2 + r;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (pos >= cbeg && pos < cend) v = *reinterpret_cast<const uint4*>(X + (size_t)pos * NCH + c * 8);
-      *reinterpret_cast<uint4*>(Xs + r * XS + c * 8) = v;
+    if (FUSE_L1) {
+      for (int i = tid; i < TPC + 8; i += blockDim.x) {
+        const int pos = pos0 - 4 + i;
+        xs[i] = (pos >= cbeg && pos < cend) ? xin[pos] : 0.f;
+      }
+      __syncthreads();
+      const int o = tid & 63;
+      for (int r = tid >> 6; r < TPC + 4; r += 2) {
+        const int pos = pos0 - 2 + r;
+        float v = 0.f;
+        if (pos >= cbeg && pos < cend) {
+          float z = b1;
+#pragma unroll
+          for (int j = 0; j < KT5; ++j) z = fmaf(w1[j], xs[r + j], z);  // x[pos + j - 2]
+          v = gelu_f(z);
+        }
+        Xs[r * XS + o] = f2bf(v);
+      }
+    } else {
+      for (int i = tid; i < (TPC + 4) * (NCH / 8); i += blockDim.x) {
+        const int r = i / (NCH / 8), c = i - r * (NCH / 8);
+        const int pos = pos0 - 2 + r;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (pos >= cbeg && pos < cend) v = *reinterpret_cast<const uint4*>(X + (size_t)pos * NCH + c * 8);
+        *reinterpret_cast<uint4*>(Xs + r * XS + c * 8) = v;
+      }
     }
     __syncthreads();
-    float acc[4][2][4];
+    float acc[4][4][4];
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
-      for (int n = 0; n < 2; ++n)
+      for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
-    const int nb = warp * 16;
 #pragma unroll 1
     for (int j = 0; j < KT5; ++j) {
 #pragma unroll
       for (int cb = 0; cb < 4; ++cb) {
         const int k0 = j * NCH + cb * 16;
-        unsigned b[2][2];
+        // B fragments of n-tiles (0,1) and (2,3): matrices (nt, k 0-7), (nt, k 8-15)
+        unsigned b[2][4];
 #pragma unroll
-        for (int n = 0; n < 2; ++n) {
-          const bf16_t* xr = Xs + (nb + n * 8 + gid + j) * XS + cb * 16 + tig * 2;
-          b[n][0] = *reinterpret_cast<const unsigned*>(xr);
-          b[n][1] = *reinterpret_cast<const unsigned*>(xr + 8);
-        }
+        for (int h = 0; h < 2; ++h)
+          ldsm_x4(b[h], Xs + (nb + h * 16 + (lm >> 1) * 8 + lr + j) * XS + cb * 16 + (lm & 1) * 8);
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-          const bf16_t* wr = Ws + (m * 16 + gid) * WS + k0 + tig * 2;
-          const unsigned a0 = *reinterpret_cast<const unsigned*>(wr);
-          const unsigned a1 = *reinterpret_cast<const unsigned*>(wr + 8 * WS);
-          const unsigned a2 = *reinterpret_cast<const unsigned*>(wr + 8);
-          const unsigned a3 = *reinterpret_cast<const unsigned*>(wr + 8 * WS + 8);
+          unsigned a[4];  // matrices (rows 0-7, k 0-7), (8-15, 0-7), (0-7, 8-15), (8-15, 8-15)
+          ldsm_x4(a, Ws + (m * 16 + (lm & 1) * 8 + lr) * WS + k0 + (lm >> 1) * 8);
 #pragma unroll
-          for (int n = 0; n < 2; ++n) mma_bf16(acc[m][n], a0, a1, a2, a3, b[n][0], b[n][1]);
+          for (int n = 0; n < 4; ++n)
+            mma_bf16(acc[m][n], a[0], a[1], a[2], a[3], b[n >> 1][(n & 1) * 2],
+                     b[n >> 1][(n & 1) * 2 + 1]);
         }
       }
     }
     // epilogue: acc[m][n][q] -> channel o = m*16 + gid (+8 for q >= 2),
     //           position nb + n*8 + tig*2 (+1 for odd q)
+    if (MODE == 0 && Zout == nullptr) {
+      // inference: GELU into the (now free) input tile, then 16-byte stores
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int o = m * 16 + gid + (q >= 2 ? 8 : 0);
+            const int pl = nb + n * 8 + tig * 2 + (q & 1);
+            Xs[pl * XS + o] = f2bf(gelu_f(acc[m][n][q] + bias[o]));
+          }
+      __syncthreads();
+      for (int i = tid; i < TPC * (NCH / 8); i += blockDim.x) {
+        const int r = i / (NCH / 8), c = i - r * (NCH / 8);
+        *reinterpret_cast<uint4*>(H + (size_t)(pos0 + r) * NCH + c * 8) =
+            *reinterpret_cast<const uint4*>(Xs + r * XS + c * 8);
+      }
+      continue;
+    }
 #pragma unroll
     for (int m = 0; m < 4; ++m)
 #pragma unroll
-      for (int n = 0; n < 2; ++n)
+      for (int n = 0; n < 4; ++n)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int o = m * 16 + gid + (q >= 2 ? 8 : 0);
@@ -162,6 +240,76 @@ __global__ void __launch_bounds__(128) k_conv64(const bf16_t* __restrict__ X,
             H[idx] = f2bf(acc[m][n][q] * gelu_grad_f(Zin[idx]));
           }
         }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Last layer (64 -> 1) on the tensor cores for inference:
+//   y[pos] = b4 + sum_{j,i} W4[i][j] h3[pos + j - 2][i]
+// as a GEMM whose A operand has two non-zero rows, the BF16 high and low parts
+// of W4 (so the weights keep ~16 bits), and whose sum the epilogue forms.
+// Same tile scheme as k_conv64 with one m-tile.
+// ---------------------------------------------------------------------------
+constexpr size_t OUT_SMEM = (size_t)(16 * WS + (TPC + 4) * XS) * sizeof(bf16_t);
+
+__global__ void __launch_bounds__(128) k_conv_out(const bf16_t* __restrict__ X,
+                                                  const bf16_t* __restrict__ Wg4,
+                                                  const float* __restrict__ th,
+                                                  float* __restrict__ y, int npos, int nT) {
+  extern __shared__ uint4 smem_u4[];
+  bf16_t* Ws = reinterpret_cast<bf16_t*>(smem_u4);
+  bf16_t* Xs = Ws + 16 * WS;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int lm = lane >> 3, lr = lane & 7;
+  for (int i = tid; i < 16 * (KDIM / 8); i += blockDim.x) {
+    const int o = i / (KDIM / 8), c = i - o * (KDIM / 8);
+    *reinterpret_cast<uint4*>(Ws + o * WS + c * 8) =
+        *reinterpret_cast<const uint4*>(Wg4 + (size_t)o * KDIM + c * 8);
+  }
+  const float b4 = th[OFF_B4];
+  const int ntiles = npos / TPC;
+  const int nb = warp * 32;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int pos0 = tile * TPC;
+    const int cbeg = (pos0 / nT) * nT, cend = cbeg + nT;
+    __syncthreads();
+    for (int i = tid; i < (TPC + 4) * (NCH / 8); i += blockDim.x) {
+      const int r = i / (NCH / 8), c = i - r * (NCH / 8);
+      const int pos = pos0 - 2 + r;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (pos >= cbeg && pos < cend) v = *reinterpret_cast<const uint4*>(X + (size_t)pos * NCH + c * 8);
+      *reinterpret_cast<uint4*>(Xs + r * XS + c * 8) = v;
+    }
+    __syncthreads();
+    float acc[4][4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[n][q] = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < KT5; ++j) {
+#pragma unroll
+      for (int cb = 0; cb < 4; ++cb) {
+        const int k0 = j * NCH + cb * 16;
+        unsigned b[2][4], a[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          ldsm_x4(b[h], Xs + (nb + h * 16 + (lm >> 1) * 8 + lr + j) * XS + cb * 16 + (lm & 1) * 8);
+        ldsm_x4(a, Ws + ((lm & 1) * 8 + lr) * WS + k0 + (lm >> 1) * 8);
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+          mma_bf16(acc[n], a[0], a[1], a[2], a[3], b[n >> 1][(n & 1) * 2], b[n >> 1][(n & 1) * 2 + 1]);
+      }
+    }
+    // rows 0 (high part) and 1 (low part) sit in lanes gid = 0 and gid = 1
+#pragma unroll
+    for (int n = 0; n < 4; ++n)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const float lo = __shfl_down_sync(0xffffffffu, acc[n][q], 4);
+        if (gid == 0) y[(size_t)pos0 + nb + n * 8 + tig * 2 + q] = acc[n][q] + lo + b4;
+      }
   }
 }
 
@@ -383,7 +531,16 @@ __global__ void k_layer1_bwd(const bf16_t* __restrict__ DZ1, const float* __rest
 // WgT[i][j*64+o] = W[o][i][4-j] (the transposed convolution as a forward one)
 __global__ void k_pack(const float* __restrict__ th, bf16_t* __restrict__ Wg2,
                        bf16_t* __restrict__ Wt2, bf16_t* __restrict__ Wg3,
-                       bf16_t* __restrict__ Wt3) {
+                       bf16_t* __restrict__ Wt3, bf16_t* __restrict__ Wg4) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 16 * KDIM;
+       idx += gridDim.x * blockDim.x) {
+    // Wg4[0][j*64 + i] = hi(W4[i][j]), Wg4[1][...] = lo, other rows zero
+    const int r = idx / KDIM, k = idx - r * KDIM;
+    const int j = k / NCH, c = k - j * NCH;
+    const float w = th[OFF_W4 + c * KT5 + j];
+    const bf16_t hi = f2bf(w);
+    Wg4[idx] = r == 0 ? hi : r == 1 ? f2bf(w - bf2f(hi)) : (bf16_t)0;
+  }
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < NCH * KDIM;
        idx += gridDim.x * blockDim.x) {
     const int r = idx / KDIM, k = idx - r * KDIM;
@@ -418,7 +575,7 @@ __global__ void k_adam(float* __restrict__ th, float* __restrict__ m, float* __r
 // ---------------------------------------------------------------------------
 struct asg_net {
   float *theta = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
-  bf16_t *wg2 = nullptr, *wt2 = nullptr, *wg3 = nullptr, *wt3 = nullptr;
+  bf16_t *wg2 = nullptr, *wt2 = nullptr, *wg3 = nullptr, *wt3 = nullptr, *wg4 = nullptr;
   double* loss = nullptr;
   int adam_t = 0;
   float gamma = 1.f;  // output scale of the learned step (see GateParams)
@@ -496,14 +653,16 @@ static int net_ensure(asg_net* n, size_t npos) {
 }
 
 static int net_pack(asg_net* n, cudaStream_t st) {
-  k_pack<<<80, 256, 0, st>>>(n->theta, n->wg2, n->wt2, n->wg3, n->wt3);
+  k_pack<<<80, 256, 0, st>>>(n->theta, n->wg2, n->wt2, n->wg3, n->wt3, n->wg4);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "pack launch");
 }
 
 static int conv_smem_attr() {
   static bool done = false;
   if (done) return ASG_OK;
-  if (cudaFuncSetAttribute(k_conv64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
+  if (cudaFuncSetAttribute(k_conv64<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv_out, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WGRAD_SMEM) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "corrector kernels: shared-memory attribute");
@@ -516,7 +675,7 @@ static int net_forward(asg_net* n, const float* x, float* y, const float* target
                        const float* mask, float inv_nmask, int npos, int nT, bool keep_z,
                        cudaStream_t st) {
   CKS_NET(conv_smem_attr());
-  const int tiles = npos / TP;
+  const int tiles = npos / TPC;
   const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
   k_layer1_fwd<<<4 * n->nsm, 256, 0, st>>>(x, n->theta, keep_z ? n->z1 : nullptr, n->h1, npos, nT);
   k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(n->h1, n->wg2, n->theta + OFF_B2, nullptr,
@@ -529,9 +688,10 @@ static int net_forward(asg_net* n, const float* x, float* y, const float* target
 }
 
 static int net_backward(asg_net* n, const float* x, int npos, int nT, cudaStream_t st) {
-  const int tiles = npos / TP;
+  const int tiles = npos / TPC;
   const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
-  const int gw = tiles < n->nsm ? tiles : n->nsm;
+  const int chunks = npos / TP;
+  const int gw = chunks < n->nsm ? chunks : n->nsm;
   // last layer: dW4, db4, dz3 -> d2
   k_layer4_bwd<<<2 * n->nsm, 256, 0, st>>>(n->dy, n->h3, n->z3, n->theta, n->d2, n->grad, npos, nT);
   // layer 3: dW3 (dz3, h2), db3, dz2 = (W3^T * dz3) GELU'(z2) -> d1
@@ -551,15 +711,14 @@ static int net_backward(asg_net* n, const float* x, int npos, int nT, cudaStream
 static int net_infer(asg_net* n, const float* x, float* y, int npos, int nT, bf16_t* a,
                      bf16_t* b, cudaStream_t st) {
   CKS_NET(conv_smem_attr());
-  const int tiles = npos / TP;
-  const int gconv = tiles < 2 * n->nsm ? tiles : 2 * n->nsm;
-  k_layer1_fwd<<<4 * n->nsm, 256, 0, st>>>(x, n->theta, nullptr, a, npos, nT);
-  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(a, n->wg2, n->theta + OFF_B2, nullptr, nullptr, b,
+  const int tiles = npos / TPC;
+  const int gconv = tiles < 3 * n->nsm ? tiles : 3 * n->nsm;
+  // layers 1 + 2 (x -> h2), layer 3 (h2 -> h3), layer 4 (h3 -> y)
+  k_conv64<0, true><<<gconv, 128, CONV_SMEM, st>>>(x, n->wg2, n->theta + OFF_B2, nullptr,
+                                                   nullptr, a, npos, nT, n->theta);
+  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(a, n->wg3, n->theta + OFF_B3, nullptr, nullptr, b,
                                              npos, nT);
-  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(b, n->wg3, n->theta + OFF_B3, nullptr, nullptr, a,
-                                             npos, nT);
-  k_layer4_fwd<<<4 * n->nsm, 256, 0, st>>>(a, n->theta, y, nullptr, nullptr, 0.f, nullptr,
-                                           nullptr, npos, nT);
+  k_conv_out<<<gconv, 128, OUT_SMEM, st>>>(b, n->wg4, n->theta, y, npos, nT);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "inference launch");
 }
 
@@ -579,6 +738,7 @@ extern "C" int asg_net_create(asg_net** out) {
             cudaMalloc(&n->wt2, NCH * KDIM * 2) == cudaSuccess &&
             cudaMalloc(&n->wg3, NCH * KDIM * 2) == cudaSuccess &&
             cudaMalloc(&n->wt3, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wg4, 16 * KDIM * 2) == cudaSuccess &&
             cudaMalloc(&n->loss, sizeof(double)) == cudaSuccess;
   if (!ok) {
     asg_net_destroy(n);
@@ -596,7 +756,8 @@ extern "C" int asg_net_destroy(asg_net* n) {
   if (!n) return ASG_OK;
   net_free_acts(n);
   net_free_inf(n);
-  void* ps[] = {n->theta, n->adam_m, n->adam_v, n->grad, n->wg2, n->wt2, n->wg3, n->wt3, n->loss};
+  void* ps[] = {n->theta, n->adam_m, n->adam_v, n->grad, n->wg2, n->wt2, n->wg3, n->wt3, n->wg4,
+                n->loss};
   for (void* p : ps) cudaFree(p);
   delete n;
   return ASG_OK;
@@ -620,8 +781,8 @@ extern "C" int asg_net_get_params(asg_net* n, float* theta, int count) {
 }
 
 static int check_batch(int ncols, int nT) {
-  if (ncols <= 0 || nT < 64 || nT % TP != 0)
-    return net_fail(ASG_ERR_SHAPE, "corrector batches need nT a multiple of 64");
+  if (ncols <= 0 || nT < TPC || nT % TPC != 0)
+    return net_fail(ASG_ERR_SHAPE, "corrector batches need nT a multiple of 128");
   return ASG_OK;
 }
 

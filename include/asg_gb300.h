@@ -234,7 +234,7 @@ int asg_flux_columns_device(const float* d_in, float* d_out, int ncols, int nT, 
  * A 1-D convolutional network along t (1 -> 64 -> 64 -> 64 -> 1 channels,
  * kernel 5, GELU, zero padding per column) whose two 64x64 layers run as BF16
  * tensor-core GEMMs with FP32 accumulation; FP32 master parameters, Adam.
- * Batches are ncols device columns of nT samples (nT a multiple of 64). */
+ * Batches are ncols device columns of nT samples (nT a multiple of 128). */
 typedef struct asg_net asg_net;
 int asg_net_param_count(void);   /* length of the FP32 parameter vector */
 int asg_net_create(asg_net** out);
@@ -258,7 +258,7 @@ int asg_net_train_step(asg_net* net, const float* d_x, const float* d_target,
 int asg_net_set_output_scale(asg_net* net, float gamma);
 
 /* Learned KT step on device columns (in -> out, ncols x nT floats, nT a
- * multiple of 64 up to 1024; in != out).  Per column: s = max|u|, the plain
+ * multiple of 128 up to 1024; in != out).  Per column: s = max|u|, the plain
  * KT sub-cycle count n_sub at cfl_target, and the steepness max|u[t+1]-u[t]|.
  * When n_sub >= min_subcycles and the steepness is at most shock_ratio * s,
  * one coarse KT step of the full dz plus the scaled correction above; otherwise

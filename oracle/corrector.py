@@ -11,7 +11,8 @@ layer, so no layer mixes samples of different columns):
     h3 = GELU(conv(h2, W3[64,64,5]) + b3)
     y  =      conv(h3, W4[1,64,5])  + b4
     conv(x, W)[o, t] = sum_i sum_j W[o, i, j] x[i, t + j - 2]
-GELU(z) = z Phi(z) (the erf form).  Loss: masked mean squared error.
+GELU(z) = z/2 (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) (the tanh form).
+Loss: masked mean squared error.
 
 There is no reference implementation of this part (the reference solver has
 no learned component); the KT targets come from the reference's KT scheme
@@ -39,16 +40,17 @@ def bf16(a):
     return np.where(np.isnan(a), a, out)
 
 
-def _erf(x):
-    return np.vectorize(math.erf, otypes=[np.float64])(x)
+_C = math.sqrt(2.0 / math.pi)
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    """GELU in its tanh form."""
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + 0.044715 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2 * math.pi)
+    t = np.tanh(_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def conv(x, W, b=None):

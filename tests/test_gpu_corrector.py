@@ -57,7 +57,7 @@ def test_gradients_match_oracle():
     theta = CR.init_params(5, last_scale=1.0)
     net = CR.Corrector(theta)
     try:
-        x, tg, mk = _batch(4, 192, 2)
+        x, tg, mk = _batch(4, 256, 2)
         d = [torch.from_numpy(a).cuda() for a in (x, tg, mk)]
         loss, g = net.train_step(*d, lr=0.0, want_grad=True)
         lr_, gr = OC.loss_and_grads(x, tg, mk, _oracle_params(theta, True))
