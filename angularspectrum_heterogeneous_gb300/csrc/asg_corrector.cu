@@ -24,6 +24,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cuda_bf16.h>
+
 #include <vector>
 
 #include "asg_internal.h"
@@ -45,11 +47,8 @@ constexpr int OFF_B4 = OFF_W4 + NCH * KT5;    // [1]
 constexpr int NPARAM = OFF_B4 + 1;            // 41793
 
 __device__ __forceinline__ bf16_t f2bf(float f) {
-  // round to nearest even (finite inputs; NaN stays NaN)
-  unsigned u = __float_as_uint(f);
-  if ((u & 0x7f800000u) == 0x7f800000u) return (bf16_t)((u >> 16) | ((u & 0xffffu) ? 0x40u : 0u));
-  u += 0x7fffu + ((u >> 16) & 1u);
-  return (bf16_t)(u >> 16);
+  // round to nearest even: one cvt.rn.bf16.f32
+  return __bfloat16_as_ushort(__float2bfloat16_rn(f));
 }
 __device__ __forceinline__ float bf2f(bf16_t h) { return __uint_as_float(((unsigned)h) << 16); }
 
