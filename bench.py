@@ -45,6 +45,11 @@ def set_grid(nx, ny, nt):
     NX, NY, NT = nx, ny, nt
     V = NX * NY * NT
 B_ALG = 48.0  # algorithmic bytes per voxel-step of the Strang path (3 stages x 2 sweeps x 8 B)
+# DRAM bytes (read + write) per voxel of one launch of each pass, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the workload's
+# options on a 256 x 256 x 1024 grid; the traffic scales with the voxel count.
+DRAM_BYTES_PER_VOXEL = {"xy_A": 8.254, "xy_B": 8.256, "xy_C": 8.394, "t_nonlin": 7.198,
+                        "t_mid": 7.195, "t_end": 7.329}
 B_SWEEP = 8.0  # algorithmic bytes per voxel of one pass (read 4 + write 4)
 METRIC = "voxel-steps/s"
 
@@ -273,7 +278,11 @@ def run_gpu_arm(args):
                 v[0] for v in stats.values()) / args.steps, "tuning": tuning}),
             "hbm_GBps_alg": value * B_ALG / 1e9,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": dom,
+                         "frac": achieved / peak,
+                         "traffic": (DRAM_BYTES_PER_VOXEL[dom] * V
+                                     if dom in DRAM_BYTES_PER_VOXEL else None),
+                         "traffic_source": "ncu dram bytes per voxel at 256x256x1024, "
+                                           "scaled to the grid", "kernel": dom,
                          "peak_source": peak_kind,
                          "step_frac": value * B_ALG / 1e9 / peak},
             "kernels": per_kernel,
