@@ -67,6 +67,28 @@ static int h2d(T* d, const T* h, size_t n, cudaStream_t st) {
   return ASG_OK;
 }
 
+// Copy between a large caller buffer on the host and the device.  The host
+// buffer is page-locked for the copy (cudaHostRegister), so that it runs at the
+// host link's rate instead of going through the driver's staging buffers, and
+// unlocked again once the copy is done; a buffer that cannot be registered
+// (already registered, for one) takes the pageable copy.
+static int copy_host(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
+                     cudaStream_t st) {
+  void* host = kind == cudaMemcpyHostToDevice ? const_cast<void*>(src) : dst;
+  bool reg = false;
+  if (bytes >= ((size_t)32 << 20)) {
+    reg = cudaHostRegister(host, bytes, cudaHostRegisterDefault) == cudaSuccess;
+    if (!reg) (void)cudaGetLastError();
+  }
+  CK(cudaMemcpyAsync(dst, src, bytes, kind, st));
+  if (reg) {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    cudaHostUnregister(host);
+    if (e != cudaSuccess) return fail(ASG_ERR_CUDA, "host copy: %s", cudaGetErrorString(e));
+  }
+  return ASG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // host FFT plan helpers
 // ---------------------------------------------------------------------------
@@ -1129,8 +1151,8 @@ static int prepare_run(asg_plan* p, const float* init, double prop_dist, double 
   CK(cudaMemsetAsync(p->d_max_cur, 0, sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_max_next, 0, sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_status_step, 0, sizeof(int), p->st));
-  CK(cudaMemcpyAsync(p->real, init, (size_t)p->ncols * p->T * sizeof(float),
-                     cudaMemcpyHostToDevice, p->st));
+  CKS(copy_host(p->real, init, (size_t)p->ncols * p->T * sizeof(float), cudaMemcpyHostToDevice,
+                p->st));
   // initial upload: iprev, stability max, forward transform
   {
     TParams t = tparams(p);
@@ -1459,8 +1481,10 @@ extern "C" int asg_get_outputs(asg_plan* p, float* field, float* pnp, float* ppp
   if (!p) return fail(ASG_ERR_ARG, "null plan");
   const int nz = p->nsteps;
   const size_t nc = p->ncols;
-  if (field)
-    CK(cudaMemcpy(field, p->real, nc * p->T * sizeof(float), cudaMemcpyDeviceToHost));
+  if (field) {
+    CKS(copy_host(field, p->real, nc * p->T * sizeof(float), cudaMemcpyDeviceToHost, p->st));
+    CK(cudaStreamSynchronize(p->st));
+  }
   if (nz > 0) {
     float* tmp = nullptr;
     CKS(dalloc(&tmp, (size_t)nz * (nc > (size_t)p->T ? nc : (size_t)p->T)));
@@ -1469,8 +1493,7 @@ extern "C" int asg_get_outputs(asg_plan* p, float* field, float* pnp, float* ppp
     for (int i = 0; i < 4; ++i) {
       if (!dsts[i]) continue;
       CKS(asg_launch_transpose(srcs[i], tmp, nz, (int)nc, p->st));
-      CK(cudaMemcpyAsync(dsts[i], tmp, (size_t)nz * nc * sizeof(float), cudaMemcpyDeviceToHost,
-                         p->st));
+      CKS(copy_host(dsts[i], tmp, (size_t)nz * nc * sizeof(float), cudaMemcpyDeviceToHost, p->st));
       CK(cudaStreamSynchronize(p->st));
     }
     if (pax) {

@@ -506,10 +506,12 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         const float2 lo = x0 > 0 ? tile[(x0 - 1) * TS + c] : make_float2(0.f, 0.f);
         const float2 hi = x0 + CHUNK < X ? tile[(x0 + CHUNK) * TS + c] : make_float2(0.f, 0.f);
         bool any = false;
+#pragma unroll
         for (int x = x0; x < x0 + CHUNK; ++x) any |= wxs[x] != 0.f;
         __syncthreads();
         if (any) {
           float2 prev = lo, cur = tile[x0 * TS + c];
+#pragma unroll 8
           for (int x = x0; x < x0 + CHUNK; ++x) {
             const float2 next = x + 1 < x0 + CHUNK ? tile[(x + 1) * TS + c] : hi;
             const float w = wxs[x];
