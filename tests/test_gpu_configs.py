@@ -27,6 +27,9 @@ def test_full_cpu_config_matches_reference_and_fp64():
     vs32 = {k: rel(got[k], ref["fp32_" + k]) for k in keys}
     vs64 = {k: rel(got[k], ref[k]) for k in keys}
     ref32 = {k: float(ref["fp32_rel_" + k]) for k in keys}
+    print("\nrel-L2 vs reference FP32:", {k: f"{v:.2e}" for k, v in vs32.items()})
+    print("rel-L2 vs FP64 oracle:", {k: f"{v:.2e}" for k, v in vs64.items()})
+    print("reference FP32 vs FP64:", {k: f"{v:.2e}" for k, v in ref32.items()})
     for k in keys:
         field = k in ("field_dec", "pax")  # pax holds field samples
         # against the reference's own (FP32) run: 1e-4 on the field, 1e-3 on pnp/ppp/pI
