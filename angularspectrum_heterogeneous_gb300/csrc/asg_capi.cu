@@ -352,9 +352,10 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
   return ASG_OK;
 }
 
-static bool g_roots_done = false;
+static bool g_roots_done[ASG_MAX_DEVICES] = {};
 static int upload_roots() {
-  if (g_roots_done) return ASG_OK;
+  const int dev = asg_device_slot();
+  if (g_roots_done[dev]) return ASG_OK;
   std::vector<float2> w192, w64;
   roots(192, w192);
   roots(64, w64);
@@ -362,7 +363,7 @@ static int upload_roots() {
       asg_roots_upload_xy(w192.data(), w64.data()) != 0 ||
       asg_roots_upload_l2(w192.data(), w64.data()) != 0)
     return fail(ASG_ERR_CUDA, "upload of the constant root tables failed");
-  g_roots_done = true;
+  g_roots_done[dev] = true;
   return ASG_OK;
 }
 

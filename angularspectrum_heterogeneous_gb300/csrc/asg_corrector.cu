@@ -657,15 +657,16 @@ static int net_pack(asg_net* n, cudaStream_t st) {
 }
 
 static int conv_smem_attr() {
-  static bool done = false;
-  if (done) return ASG_OK;
+  static bool done[ASG_MAX_DEVICES] = {};
+  const int dev = asg_device_slot();
+  if (done[dev]) return ASG_OK;
   if (cudaFuncSetAttribute(k_conv64<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv_out, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WGRAD_SMEM) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "corrector kernels: shared-memory attribute");
-  done = true;
+  done[dev] = true;
   return ASG_OK;
 }
 

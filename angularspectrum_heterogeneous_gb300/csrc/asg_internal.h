@@ -143,6 +143,16 @@ int asg_roots_upload_t(const float2* w192, const float2* w64);
 int asg_roots_upload_xy(const float2* w192, const float2* w64);
 int asg_roots_upload_l2(const float2* w192, const float2* w64);
 
+// One-time launcher set-up (shared-memory attributes, occupancy queries,
+// constant tables) is per device: what is set with one device current does not
+// carry over to another.  Launchers keep their flags per device ordinal.
+constexpr int ASG_MAX_DEVICES = 64;
+inline int asg_device_slot() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= ASG_MAX_DEVICES) d = 0;
+  return d;
+}
+
 // error reporting shared by the translation units (message for asg_last_error)
 int asg_fail_message(int code, const char* msg);
 #define CKS_NET(expr)            \

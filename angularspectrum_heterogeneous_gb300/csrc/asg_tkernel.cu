@@ -355,12 +355,13 @@ static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   constexpr bool KT_CHUNK = (2 * M + 31) / 32 <= 32;
   constexpr int EXTRA = MODE != TM_FLUX ? 0 : (KT_CHUNK ? 8 * skew_floats(2 * M) / 2 : C * LS);
   const size_t smem = (size_t)(C * LS + EXTRA + M) * sizeof(float2);
-  static bool attr_done = false;
-  if (!attr_done) {
+  static bool attr_done[ASG_MAX_DEVICES] = {};
+  const int dev = asg_device_slot();
+  if (!attr_done[dev]) {
     if (cudaFuncSetAttribute(tk_fast<PL, MODE, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return ASG_ERR_CUDA;
-    attr_done = true;
+    attr_done[dev] = true;
   }
   const int grid = (p.X / 2) * (p.Y / (C / 2));
   tk_fast<PL, MODE, C><<<grid, 256, smem, st>>>(p);

@@ -757,8 +757,16 @@ static int launch_fast_xy(const XYParams& p, cudaStream_t st) {
   constexpr int NT = (R == 32 && Yn >= 256) ? 512 : 256;
   const size_t smem = (size_t)(R * PY::PADDED + 2 * PY::PADDED + Yn + 512) * sizeof(float2) +
                       (size_t)(Yn + 2 * R) * sizeof(int);
-  static int max_clusters = -1;
-  static int cached_G = -1;
+  static int max_clusters_dev[ASG_MAX_DEVICES], cached_G_dev[ASG_MAX_DEVICES];
+  static bool init_dev[ASG_MAX_DEVICES] = {};
+  const int dev = asg_device_slot();
+  int& max_clusters = max_clusters_dev[dev];
+  int& cached_G = cached_G_dev[dev];
+  if (!init_dev[dev]) {
+    max_clusters = -1;
+    cached_G = -1;
+    init_dev[dev] = true;
+  }
   auto kern = xy_fast<PY, R, NT>;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];

@@ -664,7 +664,16 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
   p.l2_buf_elems = nbuf;
   const size_t smem = (size_t)(nbuf + Yn + Xn) * sizeof(float2) + (size_t)(Yn + 2 * Xn) * sizeof(int);
   auto kern = xy_l2<PY, PX, R, NT>;
-  static int max_clusters = -1, cached_G = -1;
+  static int max_clusters_dev[ASG_MAX_DEVICES], cached_G_dev[ASG_MAX_DEVICES];
+  static bool init_dev[ASG_MAX_DEVICES] = {};
+  const int dev = asg_device_slot();
+  int& max_clusters = max_clusters_dev[dev];
+  int& cached_G = cached_G_dev[dev];
+  if (!init_dev[dev]) {
+    max_clusters = -1;
+    cached_G = -1;
+    init_dev[dev] = true;
+  }
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -722,7 +731,14 @@ static int launch_l2c(const XYParams& pin, cudaStream_t st) {
                       (size_t)(2 * (2 * Xn) + 2 * Yn) * sizeof(float) +
                       (size_t)(Yn + 2 * Xn) * sizeof(int);
   auto kern = xy_l2c<PY, PX, R, NT>;
-  static int max_clusters = -1;
+  static int max_clusters_dev[ASG_MAX_DEVICES];
+  static bool init_dev[ASG_MAX_DEVICES] = {};
+  const int dev = asg_device_slot();
+  int& max_clusters = max_clusters_dev[dev];
+  if (!init_dev[dev]) {
+    max_clusters = -1;
+    init_dev[dev] = true;
+  }
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
