@@ -243,6 +243,208 @@ __global__ void __launch_bounds__(128) k_conv64(const void* __restrict__ Xv,
 }
 
 // ---------------------------------------------------------------------------
+// 64 -> 64 convolution for inference on the 5th-generation tensor cores
+// (tcgen05.mma, BF16 operands from shared memory, FP32 accumulator in TMEM).
+//   D[pos][o] = sum_j sum_i X[pos + j - 2][i] W[o][i][j]
+// A tile of 128 positions is one M = 128, N = 64 GEMM accumulated over 5 taps x
+// 4 channel blocks (K = 16 each): 20 MMAs issued by one thread.  Operands are
+// K-major without swizzle: the activation tile is stored K-chunk-major
+// (8 channels x 132 rows of 16 B per chunk, rows contiguous), so the tap shift
+// j is a 16 j-byte offset of the descriptor's start address and one staged
+// tile serves all five taps.  The weights of each tap are stored the same way
+// (8 chunks x 64 rows), once per CTA.  The epilogue reads the accumulator
+// with tcgen05.ld (warp w: TMEM lanes = positions 32w .. 32w+31), applies bias
+// and GELU and writes BF16 rows.  Every wait is bounded; on a timeout the
+// kernel sets *err, frees its TMEM and returns.
+// ---------------------------------------------------------------------------
+constexpr int TC_ROWS = TPC + 4;                 // staged rows pos0-2 .. pos0+129
+constexpr int TC_LBO_X = TC_ROWS * 16;           // bytes between 8-channel chunks of the tile
+constexpr int TC_W_BYTES = KT5 * 8 * NCH * 16;   // 40 KB of weights
+constexpr int TC_X_BYTES = 8 * TC_LBO_X;         // 16.5 KB of activations
+constexpr size_t TC_SMEM =
+    (size_t)TC_W_BYTES + 2 * ((size_t)TC_X_BYTES + (TPC + 8) * sizeof(float) + 64);
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  // shared-memory matrix descriptor: start, leading (K) and stride (8-row group)
+  // byte offsets in 16-byte units, descriptor version 1, no swizzle
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = 64, M = 128
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NCH >> 3) << 17) |
+                              ((uint32_t)(TPC >> 4) << 24);
+
+// barrier of one warpgroup (128 threads) of the CTA
+__device__ __forceinline__ void wg_sync(int half) {
+  asm volatile("bar.sync %0, 128;\n" ::"r"(1 + half) : "memory");
+}
+__device__ __forceinline__ bool wg_any(int half, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.or.pred q, %2, 128, p;\n"
+      "selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(1 + half)
+      : "memory");
+  return r != 0;
+}
+
+// Two warpgroups per CTA, each with its own tile stream, staging buffer,
+// mbarrier and 64 TMEM columns; the weights are shared.
+template <bool FUSE_L1>
+__global__ void __launch_bounds__(256) k_conv64_tc(const void* __restrict__ Xv,
+                                                   const bf16_t* __restrict__ Wtc,
+                                                   const float* __restrict__ bias,
+                                                   bf16_t* __restrict__ H, int npos, int nT,
+                                                   const float* __restrict__ th,
+                                                   int* __restrict__ err) {
+  extern __shared__ uint4 smem_u4[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(smem_u4);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int half = warp >> 2, ht = tid & 127;
+  unsigned char* Ws = sm;                       // [tap][chunk][64 rows][16 B]
+  unsigned char* mine = sm + TC_W_BYTES + half * (TC_X_BYTES + (TPC + 8) * sizeof(float) + 64);
+  unsigned char* Xs = mine;                     // [chunk][132 rows][16 B]
+  float* xs = reinterpret_cast<float*>(Xs + TC_X_BYTES);  // FUSE_L1: x[pos0-4 .. pos0+131]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(xs + TPC + 8);
+  __shared__ uint32_t tslot;
+  const bf16_t* X = static_cast<const bf16_t*>(Xv);
+  const float* xin = static_cast<const float*>(Xv);
+  for (int i = tid; i < TC_W_BYTES / 16; i += blockDim.x)
+    reinterpret_cast<uint4*>(Ws)[i] = reinterpret_cast<const uint4*>(Wtc)[i];
+  float w1[KT5], b1 = 0.f;
+  if (FUSE_L1) {
+#pragma unroll
+    for (int j = 0; j < KT5; ++j) w1[j] = th[OFF_W1 + (ht & 63) * KT5 + j];
+    b1 = th[OFF_B1 + (ht & 63)];
+  }
+  const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(mbar);
+  if (ht == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_a));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(
+        (uint32_t)__cvta_generic_to_shared(&tslot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tslot + (uint32_t)(half * 64);  // my 64 accumulator columns
+  const uint32_t xs_a = (uint32_t)__cvta_generic_to_shared(Xs);
+  const uint32_t ws_a = (uint32_t)__cvta_generic_to_shared(Ws);
+  const int ntiles = npos / TPC;
+  uint32_t phase = 0;
+  for (int tile = 2 * blockIdx.x + half; tile < ntiles; tile += 2 * gridDim.x) {
+    const int pos0 = tile * TPC;
+    const int cbeg = (pos0 / nT) * nT, cend = cbeg + nT;
+    // ---- stage the tile (rows pos0-2 .. pos0+129, zero outside the column) ----
+    if (FUSE_L1) {
+      for (int i = ht; i < TPC + 8; i += 128) {
+        const int pos = pos0 - 4 + i;
+        xs[i] = (pos >= cbeg && pos < cend) ? xin[pos] : 0.f;
+      }
+      wg_sync(half);
+      const int o = ht & 63;
+      for (int r = ht >> 6; r < TC_ROWS; r += 2) {
+        const int pos = pos0 - 2 + r;
+        float v = 0.f;
+        if (pos >= cbeg && pos < cend) {
+          float z = b1;
+#pragma unroll
+          for (int j = 0; j < KT5; ++j) z = fmaf(w1[j], xs[r + j], z);
+          v = gelu_f(z);
+        }
+        *reinterpret_cast<bf16_t*>(Xs + (o >> 3) * TC_LBO_X + r * 16 + (o & 7) * 2) = f2bf(v);
+      }
+    } else {
+      for (int i = ht; i < TC_ROWS * 8; i += 128) {
+        const int r = i >> 3, c = i & 7;
+        const int pos = pos0 - 2 + r;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (pos >= cbeg && pos < cend) v = *reinterpret_cast<const uint4*>(X + (size_t)pos * NCH + c * 8);
+        *reinterpret_cast<uint4*>(Xs + c * TC_LBO_X + r * 16) = v;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    wg_sync(half);
+    // ---- 20 MMAs by one thread of the warpgroup, completion to its mbarrier ----
+    if (ht == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < KT5; ++j)
+#pragma unroll
+        for (int cb = 0; cb < 4; ++cb) {
+          const uint64_t da = tc_desc(xs_a + (2 * cb) * TC_LBO_X + j * 16, TC_LBO_X, 128);
+          const uint64_t db = tc_desc(ws_a + (j * 8 + 2 * cb) * (NCH * 16), NCH * 16, 128);
+          const uint32_t acc = (j | cb) ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(da), "l"(db), "r"(TC_IDESC), "r"(acc));
+        }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar_a)
+          : "memory");
+    }
+    // ---- bounded wait for the accumulator ----
+    int ok = 0;
+    for (int it = 0; it < (1 << 20); ++it) {
+      uint32_t done;
+      asm volatile(
+          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+          "selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(mbar_a), "r"(phase)
+          : "memory");
+      if (done) {
+        ok = 1;
+        break;
+      }
+    }
+    phase ^= 1u;
+    if (wg_any(half, !ok)) {
+      if (ht == 0) atomicExch(err, 1);
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // ---- epilogue: my position's 64 channels ----
+    const int row = (warp & 3) * 32 + lane;
+    const size_t pos = (size_t)pos0 + row;
+#pragma unroll
+    for (int c0 = 0; c0 < NCH; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+          "[%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+            "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      unsigned pk[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const float lo = gelu_f(__uint_as_float(r[2 * e]) + bias[c0 + 2 * e]);
+        const float hi = gelu_f(__uint_as_float(r[2 * e + 1]) + bias[c0 + 2 * e + 1]);
+        pk[e] = (unsigned)f2bf(lo) | ((unsigned)f2bf(hi) << 16);
+      }
+      uint4* dst = reinterpret_cast<uint4*>(H + pos * NCH + c0);
+      dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    wg_sync(half);  // accumulator read and tile consumed before the next tile
+  }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tslot));
+}
+
+// ---------------------------------------------------------------------------
 // Last layer (64 -> 1) on the tensor cores for inference:
 //   y[pos] = b4 + sum_{j,i} W4[i][j] h3[pos + j - 2][i]
 // as a GEMM whose A operand has two non-zero rows, the BF16 high and low parts
@@ -530,7 +732,16 @@ __global__ void k_layer1_bwd(const bf16_t* __restrict__ DZ1, const float* __rest
 // WgT[i][j*64+o] = W[o][i][4-j] (the transposed convolution as a forward one)
 __global__ void k_pack(const float* __restrict__ th, bf16_t* __restrict__ Wg2,
                        bf16_t* __restrict__ Wt2, bf16_t* __restrict__ Wg3,
-                       bf16_t* __restrict__ Wt3, bf16_t* __restrict__ Wg4) {
+                       bf16_t* __restrict__ Wt3, bf16_t* __restrict__ Wg4,
+                       bf16_t* __restrict__ Wc2, bf16_t* __restrict__ Wc3) {
+  // tcgen05 operands: [tap j][chunk kc][row o][8 channels i]: W[o][kc*8 + e][j]
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < KT5 * NCH * NCH;
+       idx += gridDim.x * blockDim.x) {
+    const int e = idx & 7, o = (idx >> 3) & 63, jk = idx >> 9;
+    const int j = jk >> 3, i = (jk & 7) * 8 + e;
+    Wc2[idx] = f2bf(th[OFF_W2 + o * KDIM + i * KT5 + j]);
+    Wc3[idx] = f2bf(th[OFF_W3 + o * KDIM + i * KT5 + j]);
+  }
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 16 * KDIM;
        idx += gridDim.x * blockDim.x) {
     // Wg4[0][j*64 + i] = hi(W4[i][j]), Wg4[1][...] = lo, other rows zero
@@ -575,6 +786,8 @@ __global__ void k_adam(float* __restrict__ th, float* __restrict__ m, float* __r
 struct asg_net {
   float *theta = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
   bf16_t *wg2 = nullptr, *wt2 = nullptr, *wg3 = nullptr, *wt3 = nullptr, *wg4 = nullptr;
+  bf16_t *wc2 = nullptr, *wc3 = nullptr;  // tcgen05 layouts of W2, W3
+  int* tc_err = nullptr;                  // set by a tensor-core kernel whose wait timed out
   double* loss = nullptr;
   int adam_t = 0;
   float gamma = 1.f;  // output scale of the learned step (see GateParams)
@@ -652,7 +865,7 @@ static int net_ensure(asg_net* n, size_t npos) {
 }
 
 static int net_pack(asg_net* n, cudaStream_t st) {
-  k_pack<<<80, 256, 0, st>>>(n->theta, n->wg2, n->wt2, n->wg3, n->wt3, n->wg4);
+  k_pack<<<80, 256, 0, st>>>(n->theta, n->wg2, n->wt2, n->wg3, n->wt3, n->wg4, n->wc2, n->wc3);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "pack launch");
 }
 
@@ -660,7 +873,9 @@ static int conv_smem_attr() {
   static bool done[ASG_MAX_DEVICES] = {};
   const int dev = asg_device_slot();
   if (done[dev]) return ASG_OK;
-  if (cudaFuncSetAttribute(k_conv64<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
+  if (cudaFuncSetAttribute(k_conv64_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv64_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) != cudaSuccess ||
+      cudaFuncSetAttribute(k_conv64<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv_out, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OUT_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
       cudaFuncSetAttribute(k_conv64<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CONV_SMEM) != cudaSuccess ||
@@ -707,6 +922,16 @@ static int net_backward(asg_net* n, const float* x, int npos, int nT, cudaStream
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "backward launch");
 }
 
+// a tensor-core kernel gave up waiting for its accumulator (reported once)
+static int net_check_tc(asg_net* n) {
+  int e = 0;
+  if (cudaMemcpy(&e, n->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return net_fail(ASG_ERR_CUDA, "status download");
+  if (e == 0) return ASG_OK;
+  cudaMemset(n->tc_err, 0, sizeof(int));
+  return net_fail(ASG_ERR_TIMEOUT, "tensor-core accumulator wait timed out");
+}
+
 // inference: x [npos] -> y [npos] with two BF16 activation buffers
 static int net_infer(asg_net* n, const float* x, float* y, int npos, int nT, bf16_t* a,
                      bf16_t* b, cudaStream_t st) {
@@ -714,11 +939,13 @@ static int net_infer(asg_net* n, const float* x, float* y, int npos, int nT, bf1
   const int tiles = npos / TPC;
   const int gconv = tiles < 3 * n->nsm ? tiles : 3 * n->nsm;
   // layers 1 + 2 (x -> h2), layer 3 (h2 -> h3), layer 4 (h3 -> y)
-  k_conv64<0, true><<<gconv, 128, CONV_SMEM, st>>>(x, n->wg2, n->theta + OFF_B2, nullptr,
-                                                   nullptr, a, npos, nT, n->theta);
-  k_conv64<0><<<gconv, 128, CONV_SMEM, st>>>(a, n->wg3, n->theta + OFF_B3, nullptr, nullptr, b,
-                                             npos, nT);
-  k_conv_out<<<gconv, 128, OUT_SMEM, st>>>(b, n->wg4, n->theta, y, npos, nT);
+  const int gtc = (tiles + 1) / 2 < 3 * n->nsm ? (tiles + 1) / 2 : 3 * n->nsm;
+  k_conv64_tc<true><<<gtc, 256, TC_SMEM, st>>>(x, n->wc2, n->theta + OFF_B2, a, npos, nT,
+                                               n->theta, n->tc_err);
+  k_conv64_tc<false><<<gtc, 256, TC_SMEM, st>>>(a, n->wc3, n->theta + OFF_B3, b, npos, nT,
+                                                n->theta, n->tc_err);
+  const int gout = tiles < 6 * n->nsm ? tiles : 6 * n->nsm;
+  k_conv_out<<<gout, 128, OUT_SMEM, st>>>(b, n->wg4, n->theta, y, npos, nT);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "inference launch");
 }
 
@@ -739,12 +966,16 @@ extern "C" int asg_net_create(asg_net** out) {
             cudaMalloc(&n->wg3, NCH * KDIM * 2) == cudaSuccess &&
             cudaMalloc(&n->wt3, NCH * KDIM * 2) == cudaSuccess &&
             cudaMalloc(&n->wg4, 16 * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wc2, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->wc3, NCH * KDIM * 2) == cudaSuccess &&
+            cudaMalloc(&n->tc_err, sizeof(int)) == cudaSuccess &&
             cudaMalloc(&n->loss, sizeof(double)) == cudaSuccess;
   if (!ok) {
     asg_net_destroy(n);
     return net_fail(ASG_ERR_NOMEM, "corrector parameters: cudaMalloc failed");
   }
   cudaMemset(n->theta, 0, NPARAM * 4);
+  cudaMemset(n->tc_err, 0, sizeof(int));
   cudaMemset(n->adam_m, 0, NPARAM * 4);
   cudaMemset(n->adam_v, 0, NPARAM * 4);
   *out = n;
@@ -757,7 +988,7 @@ extern "C" int asg_net_destroy(asg_net* n) {
   net_free_acts(n);
   net_free_inf(n);
   void* ps[] = {n->theta, n->adam_m, n->adam_v, n->grad, n->wg2, n->wt2, n->wg3, n->wt3, n->wg4,
-                n->loss};
+                n->wc2, n->wc3, n->tc_err, n->loss};
   for (void* p : ps) cudaFree(p);
   delete n;
   return ASG_OK;
@@ -1012,5 +1243,6 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
     k_apply_correction<<<rows, 256, 0, st>>>(n->inf_y, list_col, list_s, r0, d_out, nT);
     if (cudaPeekAtLastError() != cudaSuccess) return net_fail(ASG_ERR_CUDA, "apply launch");
   }
-  return cudaStreamSynchronize(st) == cudaSuccess ? ASG_OK : net_fail(ASG_ERR_CUDA, "learned step");
+  if (cudaStreamSynchronize(st) != cudaSuccess) return net_fail(ASG_ERR_CUDA, "learned step");
+  return net_check_tc(n);
 }
