@@ -4,10 +4,10 @@
 """
 from .solver import (ASGError, Batch, Plan, SolverParams, StabilityError,  # noqa: F401
                      angular_spectrum_solve, solve_batch)
-from .sources import (generate_phase_screen, make_bowl_source,  # noqa: F401
+from .sources import (CompactPlane, generate_phase_screen, make_bowl_source,  # noqa: F401
                       make_bowl_source_planes, skull_to_phase_screens)
 
 __all__ = ["SolverParams", "angular_spectrum_solve", "solve_batch", "Plan", "Batch", "ASGError",
            "StabilityError",
-           "make_bowl_source", "make_bowl_source_planes", "generate_phase_screen",
+           "make_bowl_source", "make_bowl_source_planes", "CompactPlane", "generate_phase_screen",
            "skull_to_phase_screens"]

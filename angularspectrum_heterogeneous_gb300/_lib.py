@@ -29,7 +29,7 @@ EXPORTED = [
     "asg_batch_set_graphs", "asg_batch_run", "asg_batch_last_run_ms",
     "asg_net_param_count", "asg_net_create", "asg_net_destroy", "asg_net_set_params",
     "asg_net_get_params", "asg_net_forward", "asg_net_train_step", "asg_flux_columns_learned",
-    "asg_net_set_output_scale",
+    "asg_net_set_output_scale", "asg_add_source_compact",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -106,6 +106,7 @@ def load(require_device: bool = True):
     lib.asg_set_step_operators.argtypes = [P, C.c_int, C.POINTER(StepOps)]
     lib.asg_add_screen.argtypes = [P, C.c_double, F, F]
     lib.asg_add_source.argtypes = [P, C.c_double, F]
+    lib.asg_add_source_compact.argtypes = [P, C.c_double, C.POINTER(C.c_int), C.c_int, F]
     lib.asg_run.argtypes = [P, F, C.c_double, C.c_double, STEP_CB, P, C.POINTER(C.c_int)]
     lib.asg_get_outputs.argtypes = [P, F, F, F, F, F, _DP, F]
     lib.asg_last_run_ms.argtypes = [P, _DP]

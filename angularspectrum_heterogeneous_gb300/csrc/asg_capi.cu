@@ -779,6 +779,33 @@ extern "C" int asg_add_source(asg_plan* p, double z, const float* plane) {
   return ASG_OK;
 }
 
+extern "C" int asg_add_source_compact(asg_plan* p, double z, const int* cols, int ncols_active,
+                                      const float* values) {
+  g_err.clear();
+  if (!p || ncols_active < 0 || (ncols_active > 0 && (!cols || !values)))
+    return fail(ASG_ERR_ARG, "bad argument");
+  const int T = p->T;
+  std::vector<int> map(p->ncols, -1);
+  for (int i = 0; i < ncols_active; ++i) {
+    if (cols[i] < 0 || cols[i] >= p->ncols)
+      return fail(ASG_ERR_ARG, "source column %d outside the grid", cols[i]);
+    if (map[cols[i]] >= 0) return fail(ASG_ERR_ARG, "source column %d given twice", cols[i]);
+    map[cols[i]] = i;
+  }
+  Source s;
+  s.z = z;
+  s.nactive = ncols_active;
+  s.map = nullptr;
+  s.val = nullptr;
+  CKS(dalloc(&s.map, p->ncols));
+  CK(cudaMemcpy(s.map, map.data(), p->ncols * sizeof(int), cudaMemcpyHostToDevice));
+  CKS(dalloc(&s.val, (size_t)(ncols_active > 0 ? ncols_active : 1) * T));
+  if (ncols_active > 0)
+    CK(cudaMemcpy(s.val, values, (size_t)ncols_active * T * sizeof(float), cudaMemcpyHostToDevice));
+  p->sources.push_back(s);
+  return ASG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // kernel parameter helpers
 // ---------------------------------------------------------------------------

@@ -192,6 +192,17 @@ class Plan:
         self.n_screens += 1
 
     def add_source(self, z, plane):
+        """A dense (nX, nY, nT) source plane, or a ``sources.CompactPlane``."""
+        from .sources import CompactPlane
+        if isinstance(plane, CompactPlane):
+            assert tuple(plane.shape) == self.shape
+            cols = np.ascontiguousarray(plane.cols, dtype=np.int32)
+            vals = np.ascontiguousarray(plane.values, dtype=np.float32)
+            assert vals.shape == (cols.size, self.shape[2])
+            _lib.check(self.lib.asg_add_source_compact(
+                self.h, float(z), cols.ctypes.data_as(C.POINTER(C.c_int)), int(cols.size),
+                _lib.fptr(vals)))
+            return
         pl = np.ascontiguousarray(plane, dtype=np.float32)
         assert pl.shape == self.shape
         _lib.check(self.lib.asg_add_source(self.h, float(z), _lib.fptr(pl)))

@@ -117,6 +117,13 @@ int asg_add_screen(asg_plan* plan, double z, const float* phase, const float* am
  * its non-zero columns. */
 int asg_add_source(asg_plan* plan, double z, const float* plane);
 
+/* The same source given compact: ncols_active column indices x*nY + y and
+ * their samples values[ncols_active][nT].  An extension: no dense plane is
+ * ever formed (a 14.5 mm deep bowl on a 384x384x512 grid is ~17 GB of dense
+ * planes). */
+int asg_add_source_compact(asg_plan* plan, double z, const int* cols, int ncols_active,
+                           const float* values);
+
 /* Per-step callback: step index, z after the step, device pointer to the real
  * field (nX*nY*nT float32, valid during the call). */
 typedef void (*asg_step_cb)(void* user, int step, double z, const float* dev_field);

@@ -94,6 +94,22 @@ def test_builders_match_reference_fixtures():
     np.testing.assert_array_equal(cm, G32["gps_cmap"])
 
 
+def test_compact_bowl_planes_equal_the_dense_ones():
+    x = (np.arange(24) - 11.5) * 1.0e-3
+    y = (np.arange(20) - 9.5) * 1.2e-3
+    t = (np.arange(32) - 16) * 8e-8
+    kw = dict(inner_radius=3e-3, focus=20e-3, n_elements=3, element_delays=[0.0, 1e-7, 2e-7])
+    dense, d1 = A.make_bowl_source_planes(x, y, t, 1e6, 1540.0, 4e5, 10e-3, 25e-3, 1.0e-3, **kw)
+    comp, d2 = A.make_bowl_source_planes(x, y, t, 1e6, 1540.0, 4e5, 10e-3, 25e-3, 1.0e-3,
+                                         compact=True, **kw)
+    assert d1 == d2 and len(dense) == len(comp)
+    for (z1, p1), (z2, p2) in zip(dense, comp):
+        assert z1 == z2 and isinstance(p2, A.CompactPlane)
+        np.testing.assert_array_equal(p2.toarray(), p1)
+        nz = np.flatnonzero(np.abs(p1.reshape(-1, 32)).max(axis=1) > 0)
+        assert set(nz.tolist()) <= set(p2.cols.tolist())
+
+
 def test_tof_arguments_follow_reference_errors():
     u = np.zeros((4, 4, 8), np.float32)
     with pytest.raises(ValueError):
