@@ -95,7 +95,8 @@ def make_bowl_source_planes(xaxis, yaxis, taxis, f0, c0, p0, radius, roc, dZ, nc
     ``compact=True`` (an extension) returns each layer as a
     :class:`CompactPlane` holding only the layer's pixels, the same numbers
     as the dense plane's non-zero columns, without ever forming the dense
-    planes (~17 GB for a 384 x 384 x 512 grid and a 14.5 mm deep bowl)."""
+    planes (12 GB for a 384 x 384 x 512 grid and a 14.5 mm deep bowl sliced
+    every 0.308 mm; its active columns take 114 MB)."""
     focus = roc if focus is None else focus
     r2, r, ap, zb = _bowl_geometry(xaxis, yaxis, radius, roc, inner_radius)
     zb = np.where(ap, zb, 0.0)

@@ -475,6 +475,92 @@ def run_learned_arm(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# Transcranial bowl: compact bowl source planes and synthetic skull screens
+# ---------------------------------------------------------------------------
+def run_hetero_arm(args):
+    """Full marches (z = 0 to 80 mm) of the transcranial-bowl workload: a
+    384 x 384 x 512 grid, 39 compact bowl source planes and 30 skull screens.
+    One warm-up march, then 3 timed marches (CUDA events); the same march
+    without screens and sources is timed beside it, and the public API call
+    with host buffers gives e2e."""
+    import torch
+    import scenarios as S
+    import angularspectrum_heterogeneous_gb300 as A
+    from angularspectrum_heterogeneous_gb300.solver import _prepared_plan
+    torch.cuda.set_device(0)
+    t0 = time.time()
+    u0, kw, screens, planes = S.tips_inputs(A, compact=True)
+    t_inputs = time.time() - t0
+    vox = u0.size
+    reps = 3
+
+    def params(hetero):
+        p = A.SolverParams(**kw)
+        if hetero:
+            p.sourcePlanes, p.phaseScreens = planes, screens
+        return p
+
+    def timed(p):
+        plan, dz, steps = _prepared_plan(u0, p)
+        try:
+            plan.run(u0, p.propDist, dz)  # warm-up march
+            ms = 0.0
+            with Clocks() as clk:
+                for _ in range(reps):
+                    plan.run(u0, p.propDist, dz)
+                    ms += plan.last_run_ms()
+            launches = reps * sum(v[1] for v in plan.kernel_stats().values())  # last run's
+            plan.set_profiling(True)
+            plan.run(u0, p.propDist, dz)
+            stats = plan.kernel_stats()
+        finally:
+            plan.close()
+        return ms / reps, len(steps), launches, stats, clk.summary()
+
+    ms, nsteps, launches, stats, clocks = timed(params(True))
+    ms_homog = timed(params(False))[0]
+    # e2e: the public API with host buffers (plan, operators, screens and
+    # compact sources uploaded, march, outputs read back)
+    p = params(True)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    out = A.angular_spectrum_solve(u0, p, verbose=False)
+    torch.cuda.synchronize()
+    e2e_s = time.time() - t0
+    h2d = (u0.nbytes + sum(pl.values.nbytes + pl.cols.nbytes for _, pl in planes)
+           + sum(ph.nbytes + am.nbytes for _, ph, am in screens))
+    d2h = sum(a.nbytes for a in out)
+    peak, peak_kind = peaks()
+    value = vox * nsteps / (ms / 1e3)
+    kinds = {k: v for k, v in stats.items() if v[1] > 0 and k != "other"}
+    line = {"metric": METRIC, "value": value, "unit": "voxel-steps/s", "n_gpus": 1,
+            "steps": reps * nsteps, "warmup": nsteps, "ms_per_step": ms / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "transcranial bowl: 384x384x512, dX 3.08e-4 m, dT 4e-8 s, "
+                                   "f0 1 MHz, TIPS-like 8-element bowl (radius 46 mm, roc "
+                                   "80 mm, inner 20.5 mm, focus 50 mm, 400 kPa) as compact "
+                                   "source planes, synthetic skull shell screens at z 20-29 mm, "
+                                   "linear water, dZ = dX, propDist 80 mm (configs[2])",
+                       "grid": list(u0.shape), "march_steps": nsteps,
+                       "source_planes": len(planes), "screens": len(screens),
+                       "source_columns": int(sum(pl.cols.size for _, pl in planes)),
+                       "input_build_s": t_inputs, "parallelism": "1 GPU",
+                       "l2": "field and spectrum (302 MB each) exceed L2; no flush needed"},
+            "homogeneous_march": {"value": vox * nsteps / (ms_homog / 1e3),
+                                  "ms_per_step": ms_homog / nsteps},
+            "hbm_GBps_alg": value * B_ALG / 1e9,
+            "roofline": {"bound": "hbm", "step_frac": value * B_ALG / 1e9 / peak,
+                         "peak": peak, "peak_source": peak_kind},
+            "kernels": {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]}
+                        for k, v in kinds.items()},
+            "e2e": {"value": vox * nsteps / e2e_s, "unit": "voxel-steps/s",
+                    "h2d_bytes_per_step": h2d / nsteps, "d2h_bytes_per_step": d2h / nsteps},
+            "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,9 +572,11 @@ def main():
                     help="profiling only: a smaller grid with the same options")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "learned"],
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "batch", "learned", "hetero"],
                     help="batch: the 64-instance batched march; learned: the learned KT "
-                         "step against the plain one (neither is the headline line)")
+                         "step against the plain one; hetero: the transcranial bowl with "
+                         "skull screens (none is the headline line)")
     args = ap.parse_args()
     if args.grid:
         set_grid(*args.grid)
@@ -497,6 +585,9 @@ def main():
         return
     if args.workload == "learned" and args.impl != "reference":
         run_learned_arm(args)
+        return
+    if args.workload == "hetero" and args.impl != "reference":
+        run_hetero_arm(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -119,8 +119,9 @@ int asg_add_source(asg_plan* plan, double z, const float* plane);
 
 /* The same source given compact: ncols_active column indices x*nY + y and
  * their samples values[ncols_active][nT].  An extension: no dense plane is
- * ever formed (a 14.5 mm deep bowl on a 384x384x512 grid is ~17 GB of dense
- * planes). */
+ * ever formed (a 14.5 mm deep bowl on a 384x384x512 grid sliced every 0.308 mm
+ * is 40 dense planes, 12 GB; its active columns are 114 MB). Rejects a column
+ * outside the grid or given twice (ASG_ERR_ARG). */
 int asg_add_source_compact(asg_plan* plan, double z, const int* cols, int ncols_active,
                            const float* values);
 

@@ -103,6 +103,90 @@ def _sources(nX, nY, nT, dT, f0, zs, seed):
     return out
 
 
+def _grf(shape, spacing, corr_len, rng):
+    """Gaussian random field: white noise filtered by exp(-k^2 L^2 / 4) on the
+    FFT grid, scaled to max |g| = 1."""
+    noise = rng.standard_normal(shape)
+    k2 = 0.0
+    for ax, (n, d) in enumerate(zip(shape, spacing)):
+        k = np.fft.fftfreq(n, d) * 2 * np.pi
+        k2 = k2 + (k ** 2).reshape([-1 if a == ax else 1 for a in range(len(shape))])
+    g = np.real(np.fft.ifftn(np.fft.fftn(noise) * np.exp(-k2 * corr_len ** 2 / 4)))
+    return g / np.abs(g).max()
+
+
+def skull_shell(nX, nY, dX, dY, dz, z0=20e-3, z1=29e-3, th_min=5e-3, th_max=9e-3,
+                roc=80e-3, c_bone=2800.0, rho_bone=1900.0, porosity=0.1, corr_len=1e-3,
+                seed=0):
+    """Synthetic curved bone shell as (c, rho) maps on z-slices z0, z0+dz, ..<= z1.
+
+    The shell's near surface is a sphere of radius ``roc`` whose apex is at z0
+    on the axis; its thickness varies smoothly between th_min and th_max
+    (a 2-D random field of 15 mm correlation length); bone voxels beyond z1
+    are cut off.  In bone c = c_bone (1 + porosity g), g a 3-D random field of
+    correlation length ``corr_len`` scaled to max |g| = 1 (+-10 % by default),
+    rho = rho_bone; elsewhere c = C0, rho = RHO0.  Returns (c, rho) as
+    float64 (nX, nY, nz)."""
+    rng = np.random.default_rng(seed)
+    nz = int(np.floor((z1 - z0) / dz + 1e-9)) + 1
+    x = (np.arange(nX) - (nX - 1) / 2.0) * dX
+    y = (np.arange(nY) - (nY - 1) / 2.0) * dY
+    r2 = x[:, None] ** 2 + y[None, :] ** 2
+    sag = roc - np.sqrt(np.maximum(roc ** 2 - r2, 0.0))
+    th = th_min + (th_max - th_min) * 0.5 * (1 + _grf((nX, nY), (dX, dY), 15e-3, rng))
+    z = z0 + np.arange(nz) * dz
+    near = z0 + sag
+    bone = (z[None, None, :] >= near[:, :, None]) & (z[None, None, :] < (near + th)[:, :, None])
+    bone &= (r2 < roc ** 2)[:, :, None]
+    g = _grf((nX, nY, nz), (dX, dY, dz), corr_len, rng)
+    c = np.where(bone, c_bone * (1 + porosity * g), C0)
+    rho = np.where(bone, rho_bone, RHO0)
+    return c, rho
+
+
+# The transcranial-bowl workload: a TIPS-like annular bowl (radius 46 mm, roc
+# 80 mm, inner radius 20.5 mm, 8 elements, 400 kPa, focus 50 mm) sliced into
+# source planes, and skull screens of a synthetic shell at z = 20-29 mm, on a
+# 384 x 384 x 512 grid with dX = dY = 3.08e-4 m, dT = 4e-8 s, f0 = 1 MHz.  The
+# solver options follow the reference's own bowl example
+# (``validate_bowl.py:222-290``): linear water (beta 0, alpha0 -1), Strang,
+# adaptive filtering, standard Rusanov, Wendland taper with boundaryFactor
+# 0.15, frequency-weighted and super-absorbing (strength 0.5) boundaries,
+# dZ = dX, propDist 80 mm.
+TIPS = dict(grid=(384, 384, 512), dX=3.08e-4, dT=4e-8, f0=1e6, p0=4e5, radius=46e-3,
+            roc=80e-3, inner=20.5e-3, n_elements=8, focus=50e-3, shell_z=(20e-3, 29e-3),
+            shell_th=(5e-3, 9e-3), shell_roc=80e-3, prop=80e-3)
+
+
+def tips_inputs(builders, compact=True, **over):
+    """(initial field, SolverParams keyword dict, phase screens, source planes)
+    of the transcranial-bowl workload; ``over`` replaces entries of TIPS (the
+    tests scale it down).  ``builders`` provides make_bowl_source_planes and
+    skull_to_phase_screens (the package, or the reference's module)."""
+    g = dict(TIPS, **over)
+    nX, nY, nT = g["grid"]
+    dX, dT, f0 = g["dX"], g["dT"], g["f0"]
+    x = np.arange(nX) * dX - (nX - 1) * dX / 2
+    y = np.arange(nY) * dX - (nY - 1) * dX / 2
+    t = np.arange(nT) * dT - (nT - 1) * dT / 2
+    kw = dict(compact=True) if compact else {}
+    planes, _ = builders.make_bowl_source_planes(
+        x, y, t, f0, C0, g["p0"], g["radius"], g["roc"], dX, focus=g["focus"],
+        inner_radius=g["inner"], n_elements=g["n_elements"], **kw)
+    z0, z1 = g["shell_z"]
+    c, rho = skull_shell(nX, nY, dX, dX, dX, z0, z1, g["shell_th"][0], g["shell_th"][1],
+                         g["shell_roc"])
+    screens = [(z0 + z, ph, amp) for z, ph, amp in
+               builders.skull_to_phase_screens(c, dX, dX, C0, f0, rho_map=rho, rho0=RHO0)]
+    first = planes[0][1]
+    u0 = first.toarray() if hasattr(first, "toarray") else first
+    kw = dict(dX=dX, dY=dX, dT=dT, c0=C0, rho0=RHO0, beta=0.0, alpha0=-1.0, f0=f0,
+              propDist=g["prop"], boundaryFactor=0.15, useSplitStep=True,
+              useAdaptiveFiltering=True, useTVD=False, dZmin=dX, boundaryProfile="wendland",
+              useFreqWeightedBoundary=True, useSuperAbsorbing=True, superAbsorbingStrength=0.5)
+    return u0, kw, screens, planes[1:]
+
+
 BASE = dict(dX=2.5e-4, dY=2.5e-4, dT=4.0e-8, c0=C0, rho0=RHO0, beta=3.5, alpha0=0.5,
             attenPow=1.0, f0=2.0e6, dZmin=2.5e-4, propDist=2.0e-3)
 

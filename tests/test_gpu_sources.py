@@ -55,3 +55,29 @@ def test_compact_entry_rejects_bad_columns():
                                              u0.shape))
     finally:
         plan.close()
+
+
+# the transcranial-bowl workload scaled down to a 64 x 64 x 128 grid: a 3-element
+# bowl (radius 8 mm, roc 16 mm) and a 1-2 mm shell at z = 3.5-5.5 mm
+SMALL_TIPS = dict(grid=(64, 64, 128), radius=8e-3, roc=16e-3, inner=3.5e-3, n_elements=3,
+                  focus=10e-3, shell_z=(3.5e-3, 5.5e-3), shell_th=(1e-3, 2e-3),
+                  shell_roc=16e-3, prop=8e-3)
+
+
+def test_transcranial_bowl_vs_oracle():
+    import scenarios as S
+    import oracle.asm_oracle as O
+    from gpu_helpers import TOL, oracle_params, rel
+    u0, kw, screens, planes = S.tips_inputs(A, compact=True, **SMALL_TIPS)
+    _, _, _, dense = S.tips_inputs(A, compact=False, **SMALL_TIPS)
+    assert len(screens) >= 4 and len(planes) >= 4
+    res = A.angular_spectrum_solve(u0, solver_params(kw, {"sourcePlanes": planes,
+                                                          "phaseScreens": screens}),
+                                   verbose=False)
+    ref = O.solve(u0, oracle_params(kw, {"sourcePlanes": dense, "phaseScreens": screens}),
+                  "fp64")
+    for k, a, r in zip(KEYS, res, ref):
+        if k == "zaxis":
+            np.testing.assert_array_equal(a, r)
+            continue
+        assert rel(a, r) < TOL[k], (k, rel(a, r))
