@@ -255,16 +255,21 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     else __syncthreads();
 
     // ---- 3. my rows back from the scratch, inverse y FFT, store ----
-    for (int r = warp; r < R; r += NW) {
-      const float4* srcr = reinterpret_cast<const float4*>(S + (size_t)(rank * R + r) * Y);
+    // (cp.async.cg reads L2: other CTAs wrote these rows; each warp copies and
+    // then transforms only its own rows)
+#pragma unroll
+    for (int j = 0; j < RPW; ++j) {
+      const int r = warp + NW * j;
+      const float2* srcr = S + (size_t)(rank * R + r) * Y;
       float2* row = buf + r * RS;
-      for (int s2 = lane; s2 < Y / 2; s2 += 32)  // L2 only: other CTAs wrote these
-        *reinterpret_cast<float4*>(row + PY::pos(2 * s2)) = __ldcg(srcr + s2);
+      for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(row + PY::pos(2 * s2), srcr + 2 * s2);
     }
+    cp_async_commit();
     int qn = q + ncl;
     while (qn < nq && zero_plane(qn)) qn += ncl;
     const bool pref = qn < nq;
-    __syncthreads();
+    cp_async_wait_all();
+    __syncwarp();
     float2* gbase = sub_base(q) + (size_t)rank * R * Y;
     for (int i = lane; i < RPW * PY::N1; i += 32) {
       const int j = i / PY::N1, ka = i - j * PY::N1;
@@ -547,11 +552,13 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
 #pragma unroll
       for (int j = 0; j < RPW; ++j) {
         const int r = warp + NW * j;
-        const float4* srcr = reinterpret_cast<const float4*>(S + (size_t)(h * Xs + rank * R + r) * Y);
+        const float2* srcr = S + (size_t)(h * Xs + rank * R + r) * Y;
         float2* row = buf + r * RS;
-        for (int s2 = lane; s2 < Y / 2; s2 += 32)  // L2 only: other CTAs wrote these
-          *reinterpret_cast<float4*>(row + PY::pos(2 * s2)) = __ldcg(srcr + s2);
+        for (int s2 = lane; s2 < Y / 2; s2 += 32)  // cp.async.cg reads L2: other CTAs wrote these
+          cp_async16(row + PY::pos(2 * s2), srcr + 2 * s2);
       }
+      cp_async_commit();
+      cp_async_wait_all();
       __syncwarp();
       for (int i = lane; i < RPW * PY::N1; i += 32) {
         const int j = i / PY::N1, ka = i - j * PY::N1;
