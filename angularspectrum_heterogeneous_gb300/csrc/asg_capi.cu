@@ -208,6 +208,11 @@ struct asg_plan {
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
+  int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
+                              // 1 thread-block cluster, 2 counters in a cooperative launch
+  int batch_refs = 0;         // batches holding the plan (they use cluster barriers)
+  unsigned* grp_cnt = nullptr;  // [L2_MAX_CLUSTERS] counters of the cooperative launch
+  unsigned barrier_skew = 0;    // test hook: added to the group-barrier targets
   // CUDA graph of a regular march step (slot 0, no screen, source, callback,
   // profiling or output write); rebuilt when `gen` moves on
   bool use_graphs = true;
@@ -336,7 +341,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.val);
   }
   if (p->step_graph) cudaGraphExecDestroy(p->step_graph);
-  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->spec, p->spec2, p->nyq_tmp, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->grp_cnt, p->spec, p->spec2, p->nyq_tmp, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
@@ -502,6 +507,7 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
       }
     CKS(dalloc(&p->l2_cls_x, 2 * Xs));
     CKS(h2d(p->l2_cls_x, cl.data(), 2 * Xs, p->st));
+    CKS(dalloc(&p->grp_cnt, L2_MAX_CLUSTERS));
   }
   CKS(dalloc(&p->real, (size_t)p->ncols * T));
   std::vector<float2> w;
@@ -841,6 +847,17 @@ static TParams tparams(asg_plan* p) {
   return t;
 }
 
+// Group barrier of the L2 plane kernels: by default the counter barrier of a
+// cooperative launch for groups of 8 CTAs and more (clusters that large leave
+// SMs idle, since a cluster must fit in one GPC), thread-block clusters for
+// smaller groups and inside a batch, whose plans run side by side.
+static int xy_sync_of(const asg_plan* p) {
+  if (!p->l2) return 0;
+  if (p->batch_refs > 0) return 1;
+  if (p->xy_sync != 0) return p->xy_sync;
+  return p->G >= 8 ? 2 : 1;
+}
+
 static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   XYParams x;
   memset(&x, 0, sizeof(x));
@@ -882,6 +899,9 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.l2_cls_x = p->l2_cls_x;
   x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
                           ? p->xy_clusters : L2_MAX_CLUSTERS;
+  x.coop = xy_sync_of(p) == 2 ? 1 : 0;
+  x.grp_cnt = p->grp_cnt;
+  x.grp_skew = p->barrier_skew;
   x.skip_plane = -1;
   return x;
 }
@@ -1288,6 +1308,10 @@ extern "C" int asg_batch_create(asg_plan* const* plans, int n, asg_batch** out) 
   }
   asg_batch* b = new asg_batch();
   b->plans.assign(plans, plans + n);
+  for (int i = 0; i < n; ++i) {
+    plans[i]->batch_refs++;
+    plans[i]->gen++;  // step graphs are captured again with cluster barriers
+  }
   auto cleanup = [&](int code, const char* what) {
     cudaError_t e = cudaGetLastError();
     if (b->master) cudaStreamDestroy(b->master);
@@ -1295,6 +1319,10 @@ extern "C" int asg_batch_create(asg_plan* const* plans, int n, asg_batch** out) 
       if (ev) cudaEventDestroy(ev);
     for (auto ev : b->join) cudaEventDestroy(ev);
     for (auto ev : b->join_cap) cudaEventDestroy(ev);
+    for (asg_plan* q : b->plans) {
+      q->batch_refs--;
+      q->gen++;
+    }
     delete b;
     return fail(code, "%s: %s", what, cudaGetErrorString(e));
   };
@@ -1325,6 +1353,10 @@ extern "C" int asg_batch_destroy(asg_batch* b) {
   for (cudaEvent_t ev : {b->fork, b->fork_cap, b->ev0, b->ev1}) cudaEventDestroy(ev);
   for (auto ev : b->join) cudaEventDestroy(ev);
   for (auto ev : b->join_cap) cudaEventDestroy(ev);
+  for (asg_plan* q : b->plans) {
+    q->batch_refs--;
+    q->gen++;
+  }
   delete b;
   return ASG_OK;
 }
@@ -1566,6 +1598,7 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   out->xy_clusters = p->l2 ? ncl : 0;
   ncl = p->xy_clusters_c > 0 ? p->xy_clusters_c : L2_MAX_CLUSTERS;
   out->xy_clusters_closing = p->l2 ? ncl : 0;
+  out->xy_sync = xy_sync_of(p);
   return ASG_OK;
 }
 
@@ -1583,9 +1616,11 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
       t->xy_clusters_closing < 0 || t->xy_clusters_closing > L2_MAX_CLUSTERS)
     return fail(ASG_ERR_ARG, "cluster caps %d, %d outside 0..%d", t->xy_clusters,
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
+  if (t->xy_sync < 0 || t->xy_sync > 2) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..2", t->xy_sync);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
+  p->xy_sync = t->xy_sync;
   p->gen++;
   return ASG_OK;
 }
@@ -1627,6 +1662,26 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
       p->t_cols[i] = best_c;
     }
   }
+  if (p->l2 && status == ASG_OK && p->batch_refs == 0) {
+    // group barrier: the plain diffraction pass and the closing pass together
+    const bool closing = p->cfg.freq_weighted || p->cfg.super_absorbing;
+    double best = 1e300;
+    int best_s = 0;
+    for (int sy : {1, 2}) {
+      p->xy_sync = sy;
+      double ms = 0.0, ms_c = 0.0;
+      status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);
+      if (status != ASG_OK) break;
+      if (closing) {
+        ms_c = p->launches[ASG_K_XY_C] > 0 ? p->kms[ASG_K_XY_C] / p->launches[ASG_K_XY_C] : 0.0;
+      }
+      if (ms + ms_c < best) {
+        best = ms + ms_c;
+        best_s = sy;
+      }
+    }
+    p->xy_sync = best_s;
+  }
   if (p->l2 && status == ASG_OK) {
     double best = 1e300;
     int best_n = 0;
@@ -1663,6 +1718,13 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
   p->gen++;
   if (status != ASG_OK) return status;
   return chosen ? asg_get_tuning(p, chosen) : ASG_OK;
+}
+
+extern "C" int asg_debug_set_barrier_skew(asg_plan* p, int skew) {
+  if (!p || skew < 0) return fail(ASG_ERR_ARG, "bad argument");
+  p->barrier_skew = (unsigned)skew;
+  p->gen++;
+  return ASG_OK;
 }
 
 extern "C" int asg_last_run_ms(asg_plan* p, double* ms) {

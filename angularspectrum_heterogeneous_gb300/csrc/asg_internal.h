@@ -96,6 +96,10 @@ struct XYParams {
   const int* l2_cls_x;     // [nsub][Xs] class of each x slot of the Xs-point FFT
   int l2_buf_elems;        // set by the launcher
   int l2_max_clusters;     // clusters the scratch was sized for
+  int coop;                // 1: CTA groups of a cooperative launch synchronised by
+                           //    counters in grp_cnt instead of thread-block clusters
+  unsigned* grp_cnt;       // [l2_max_clusters] arrival counters (zeroed by the launcher)
+  unsigned grp_skew;       // added to every barrier target (test hook: 0 in normal runs)
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
 };
 

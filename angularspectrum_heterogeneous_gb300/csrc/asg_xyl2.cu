@@ -54,6 +54,46 @@ ASG_DEV bool l2_should_skip(const XYParams& p) {
   return false;
 }
 
+ASG_DEV unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Barrier of the G CTAs of one group when the kernel runs as a cooperative
+// launch (every CTA of the grid is resident) instead of thread-block
+// clusters: CTA arrivals are counted in global memory, with fences on both
+// sides so that the group's scratch writes before the barrier are visible to
+// its reads after it (the reads go to L2: cp.async.cg).  `target` is G times
+// the number of barriers passed so far.  The wait gives up after one second,
+// or as soon as the status word is set, records ASG_ERR_TIMEOUT (if nothing
+// else was recorded) and returns false; the caller then leaves the kernel.
+ASG_DEV bool group_barrier(unsigned* cnt, unsigned target, unsigned* status, int* ok_s) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    atomicAdd(cnt, 1u);
+    const unsigned long long t0 = global_ns();
+    while (*((volatile unsigned*)cnt) < target) {
+      if (*((volatile unsigned*)status) != 0u) {
+        ok = 0;
+        break;
+      }
+      if (global_ns() - t0 > 1000000000ull) {
+        atomicCAS(status, 0u, (unsigned)(-ASG_ERR_TIMEOUT));
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    *ok_s = ok;
+  }
+  __syncthreads();
+  return *ok_s != 0;
+}
+
 }  // namespace
 
 template <class PY, class PX, int R, int NT>
@@ -79,9 +119,22 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   int* clsx = clsy + Y;               // [nsub][Xs] by x slot of the Xs-point FFT
 
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (G > 1) ? (int)cl.block_rank() : 0;
+  const bool coop = p.coop != 0;
+  const int rank = coop ? (int)(blockIdx.x % G) : (G > 1) ? (int)cl.block_rank() : 0;
   const int cid = blockIdx.x / G, ncl = gridDim.x / G;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  __shared__ int sync_ok;
+  unsigned arrivals = 0;
+  // the group barrier: cluster barrier, or the counter barrier of a cooperative launch
+  auto gsync = [&]() -> bool {
+    if (coop) {
+      arrivals += G;
+      return group_barrier(p.grp_cnt + cid, arrivals + p.grp_skew, p.status, &sync_ok);
+    }
+    if (G > 1) cl.sync();
+    else __syncthreads();
+    return true;
+  };
   const int nsub = p.nsub;
   const int nq = p.nplanes * nsub;
   if (l2_should_skip(p)) return;
@@ -147,10 +200,9 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int s2 = lane; s2 < Y / 2; s2 += 32)
         dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
     }
-    // the cluster barrier's arrive (release) / wait (acquire) pair orders these
-    // global writes before the other CTAs' reads of the scratch
-    if (G > 1) cl.sync();
-    else __syncthreads();
+    // the barrier (release / acquire) orders these global writes before the
+    // other CTAs' reads of the scratch
+    if (!gsync()) break;
 
     // ---- 2. columns [rank*Yc, +Yc) of all Xs rows: x FFT, multiplier, inverse ----
     {
@@ -228,8 +280,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
           atomicAdd(p.power_acc + 1, b);
         }
         // no CTA reuses the scratch before every CTA has read it
-        if (G > 1) cl.sync();
-        else __syncthreads();
+        if (!gsync()) break;
         continue;
       }
       __syncthreads();
@@ -251,8 +302,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
             *reinterpret_cast<const float4*>(buf + x * TS + c2);
       }
     }
-    if (G > 1) cl.sync();
-    else __syncthreads();
+    if (!gsync()) break;
 
     // ---- 3. my rows back from the scratch, inverse y FFT, store ----
     // (cp.async.cg reads L2: other CTAs wrote these rows; each warp copies and
@@ -358,10 +408,22 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
   int* clsx = clsy + Y;                               // [2][Xs]
 
   cg::cluster_group cl = cg::this_cluster();
-  const int rank = (G > 1) ? (int)cl.block_rank() : 0;
+  const bool coop = p.coop != 0;
+  const int rank = coop ? (int)(blockIdx.x % G) : (G > 1) ? (int)cl.block_rank() : 0;
   const int cid = blockIdx.x / G, ncl = gridDim.x / G;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (*((volatile const unsigned*)p.status) != 0u) return;
+  __shared__ int sync_ok;
+  unsigned arrivals = 0;
+  auto gsync = [&]() -> bool {
+    if (coop) {
+      arrivals += G;
+      return group_barrier(p.grp_cnt + cid, arrivals + p.grp_skew, p.status, &sync_ok);
+    }
+    if (G > 1) cl.sync();
+    else __syncthreads();
+    return true;
+  };
 
   for (int i = tid; i < Y; i += NT) {
     tw_y[i] = p.twY[i];
@@ -425,8 +487,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
       }
       __syncwarp();  // my rows are reloaded next
     }
-    if (G > 1) cl.sync();
-    else __syncthreads();
+    if (!gsync()) break;
 
     // ---- 2. per round: x FFT, multiplier, inverse, recombination, x edges ----
 #pragma unroll 1
@@ -543,8 +604,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
       }
       __syncthreads();  // tile reused by the next round
     }
-    if (G > 1) cl.sync();
-    else __syncthreads();
+    if (!gsync()) break;
 
     // ---- 3. my whole-plane rows: inverse y FFT, y edges, screens, store ----
 #pragma unroll 1
@@ -659,6 +719,42 @@ bool asg_xy_l2_supported(int X, int Y, int nsub, int* G_out) {
   return true;
 }
 
+// Groups of G CTAs that a cooperative launch keeps resident at once.
+template <class K>
+static int coop_max_groups(K kern, int nt, size_t smem, int G) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem) != cudaSuccess)
+    return 0;
+  return per_sm * nsm / G;
+}
+
+// Launches `units` (sub-)planes over at most `resident` groups (clusters, or
+// CTA groups of a cooperative launch) and the scratch the plan sized.
+template <class K>
+static int launch_groups(K kern, const XYParams& p, cudaLaunchConfig_t cfg, int resident,
+                         int units, cudaStream_t st) {
+  int ng = resident < units ? resident : units;
+  if (ng > p.l2_max_clusters) ng = p.l2_max_clusters;
+  if (ng < 1) return ASG_ERR_SHAPE;
+  cudaLaunchAttribute coop[1];
+  if (p.coop) {
+    if (p.grp_cnt == nullptr) return ASG_ERR_ARG;
+    // every CTA of the grid is resident, so the counter barriers of a group
+    // always complete
+    if (cudaMemsetAsync(p.grp_cnt, 0, (size_t)ng * sizeof(unsigned), st) != cudaSuccess)
+      return ASG_ERR_CUDA;
+    coop[0].id = cudaLaunchAttributeCooperative;
+    coop[0].val.cooperative = 1;
+    cfg.attrs = coop;
+    cfg.numAttrs = 1;
+  }
+  cfg.gridDim = dim3(p.G * ng, 1, 1);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
+  return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+}
+
 template <int Yn, int Xn>
 static int launch_l2(const XYParams& pin, cudaStream_t st) {
   using PY = FastPlan<Yn>;
@@ -692,6 +788,8 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  static int max_groups_dev[ASG_MAX_DEVICES];
+  int& max_groups = max_groups_dev[dev];
   if (max_clusters < 0 || cached_G != p.G) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
@@ -701,14 +799,11 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) n = 1;
     max_clusters = n;
+    max_groups = coop_max_groups(kern, NT, smem, p.G);
     cached_G = p.G;
   }
   const int nq = p.nplanes * p.nsub;
-  int ncl = max_clusters < nq ? max_clusters : nq;
-  if (ncl > p.l2_max_clusters) ncl = p.l2_max_clusters;
-  cfg.gridDim = dim3(p.G * ncl, 1, 1);
-  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
-  return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+  return launch_groups(kern, p, cfg, p.coop ? max_groups : max_clusters, nq, st);
 }
 
 int asg_launch_xy_l2(const XYParams& p, cudaStream_t st) {
@@ -757,6 +852,8 @@ static int launch_l2c(const XYParams& pin, cudaStream_t st) {
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  static int max_groups_dev[ASG_MAX_DEVICES];
+  int& max_groups = max_groups_dev[dev];
   if (max_clusters < 0) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
@@ -766,12 +863,9 @@ static int launch_l2c(const XYParams& pin, cudaStream_t st) {
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) n = 1;
     max_clusters = n;
+    max_groups = coop_max_groups(kern, NT, smem, G);
   }
-  int ncl = max_clusters < p.nplanes ? max_clusters : p.nplanes;
-  if (ncl > p.l2_max_clusters) ncl = p.l2_max_clusters;
-  cfg.gridDim = dim3(G * ncl, 1, 1);
-  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
-  return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+  return launch_groups(kern, p, cfg, p.coop ? max_groups : max_clusters, p.nplanes, st);
 }
 
 int asg_launch_xy_l2_closing(const XYParams& p, cudaStream_t st) {

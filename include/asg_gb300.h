@@ -196,7 +196,15 @@ typedef struct {
   int t_cols_stats;  /* columns per block of the column pass closing a step: 8, 16 */
   int xy_clusters;   /* cap on resident clusters of the L2-exchange plane kernel: 0..32 */
   int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..32 */
+  int xy_sync;       /* group barrier of those kernels: 1 thread-block cluster, 2 counter
+                      * barrier in a cooperative launch (plans in a batch use 1) */
 } asg_tuning;
+
+/* Test hook (no counterpart in the reference): adds `skew` to every target of
+ * the counter barriers of the cooperative plane kernels (xy_sync = 2), so that
+ * their bounded waits (one second) run out and the run ends with
+ * ASG_ERR_TIMEOUT; 0 restores normal operation. */
+int asg_debug_set_barrier_skew(asg_plan* plan, int skew);
 
 /* Effective launch shapes (defaults resolved). */
 int asg_get_tuning(asg_plan* plan, asg_tuning* out);

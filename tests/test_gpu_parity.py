@@ -155,6 +155,12 @@ FAST_CASES = {
     "kt_fw_sa_64x128": ((64, 128, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                              useSuperAbsorbing=True), 8e6, 10),
     "lie_water_96": ((96, 96, 192), dict(useSplitStep=False, alpha0=-1.0), 3e6, 8),
+    # groups of 8 CTAs: plane kernels in a cooperative launch with counter barriers,
+    # with the beam-obliquity power pass (its extra barrier) in the second case
+    "kt_fw_sa_256_coop": ((256, 256, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
+                                                useSuperAbsorbing=True), 4e6, 2),
+    "kt_obl_256_coop": ((256, 256, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
+                        4e6, 2),
     "kt_obl_32x64": ((32, 64, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
                      6e6, 8),
     # half-plane (split-x) kernels with the beam-obliquity power pass

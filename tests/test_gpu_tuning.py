@@ -25,7 +25,7 @@ def _run(plan, u0, dz, steps=3):
 
 
 @pytest.mark.parametrize("shape,flux", [((32, 128, 1024), "kt"), ((64, 128, 256), "rusanov"),
-                                        ((32, 64, 512), "kt")])
+                                        ((32, 64, 512), "kt"), ((256, 256, 256), "kt")])
 def test_every_shape_gives_the_same_march(shape, flux):
     from angularspectrum_heterogeneous_gb300 import Plan
     from angularspectrum_heterogeneous_gb300.solver import initial_step
@@ -37,19 +37,22 @@ def test_every_shape_gives_the_same_march(shape, flux):
         ref = _run(plan, u0, dz)
         default = plan.get_tuning()
         shapes = [dict(t_cols_flux=8, t_cols_plain=8, t_cols_stats=8, xy_clusters=0,
-                       xy_clusters_closing=2),
+                       xy_clusters_closing=2, xy_sync=1),
                   dict(t_cols_flux=16, t_cols_plain=16, t_cols_stats=16, xy_clusters=3,
-                       xy_clusters_closing=0)]
+                       xy_clusters_closing=0, xy_sync=2),
+                  dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
+                       xy_clusters_closing=0, xy_sync=2)]
         for tun in shapes:
             plan.set_tuning(tun)
             got = plan.get_tuning()
             for k in ("t_cols_flux", "t_cols_plain", "t_cols_stats"):
-                assert got[k] == tun[k]
+                assert tun[k] == 0 or got[k] == tun[k]
+            assert got["xy_sync"] == (tun["xy_sync"] if default["xy_sync"] else 0)
             out = _run(plan, u0, dz)
             for k, a, b in zip(KEYS, ref, out):
                 assert np.array_equal(a, b), (tun, k)
         plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
-                             xy_clusters_closing=0))
+                             xy_clusters_closing=0, xy_sync=0))
         assert plan.get_tuning() == default
     finally:
         plan.close()
@@ -69,6 +72,41 @@ def test_unsupported_shape_is_rejected():
             plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=99))
     finally:
         plan.close()
+
+
+def test_group_barrier_wait_runs_out_and_the_plan_recovers():
+    """The counter barriers of the cooperative plane kernels are bounded: with
+    a target no group reaches, every wait gives up after a second, the run
+    ends with ASG_ERR_TIMEOUT, and the next run (normal targets) matches the
+    earlier one bit for bit."""
+    from angularspectrum_heterogeneous_gb300 import Plan
+    from angularspectrum_heterogeneous_gb300._lib import ASGError
+    from angularspectrum_heterogeneous_gb300.solver import initial_step
+    shape = (256, 256, 128)
+    params, u0 = _case(shape)
+    dz = initial_step(u0, params)
+    plan = Plan(shape, params)
+    try:
+        plan.set_operators(0, dz)
+        plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
+                             xy_clusters_closing=0, xy_sync=2))
+        assert plan.get_tuning()["xy_sync"] == 2
+        ref = _run(plan, u0, dz, steps=2)
+        _lib_check(plan, 1)
+        with pytest.raises(ASGError) as e:
+            _run(plan, u0, dz, steps=2)
+        assert e.value.code == -5  # ASG_ERR_TIMEOUT
+        _lib_check(plan, 0)
+        out = _run(plan, u0, dz, steps=2)
+        for k, a, b in zip(KEYS, ref, out):
+            assert np.array_equal(a, b), k
+    finally:
+        plan.close()
+
+
+def _lib_check(plan, skew):
+    from angularspectrum_heterogeneous_gb300 import _lib
+    _lib.check(plan.lib.asg_debug_set_barrier_skew(plan.h, skew))
 
 
 def test_autotune_picks_a_supported_shape_and_keeps_the_result():
