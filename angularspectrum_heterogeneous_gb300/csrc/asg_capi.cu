@@ -121,7 +121,7 @@ static void roots(int n, std::vector<float2>& out) {
   }
 }
 
-static constexpr int L2_MAX_CLUSTERS = 32;
+static constexpr int L2_MAX_CLUSTERS = 64;
 
 // four-step slot order of a fast line of length n (n = n1*n2)
 static void fast_factors(int n, int* n1, int* n2) {
@@ -848,14 +848,15 @@ static TParams tparams(asg_plan* p) {
 }
 
 // Group barrier of the L2 plane kernels: by default the counter barrier of a
-// cooperative launch for groups of 8 CTAs and more (clusters that large leave
-// SMs idle, since a cluster must fit in one GPC), thread-block clusters for
-// smaller groups and inside a batch, whose plans run side by side.
+// cooperative launch for groups of 16 CTAs (16-CTA clusters leave SMs idle,
+// since a cluster must fit in one GPC: 14 of them are resident on a GB300,
+// 224 of 304 CTA slots), thread-block clusters for smaller groups, which pack
+// well and measure faster, and inside a batch, whose plans run side by side.
 static int xy_sync_of(const asg_plan* p) {
   if (!p->l2) return 0;
   if (p->batch_refs > 0) return 1;
   if (p->xy_sync != 0) return p->xy_sync;
-  return p->G >= 8 ? 2 : 1;
+  return p->G >= 16 ? 2 : 1;
 }
 
 static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {

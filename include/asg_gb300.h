@@ -194,8 +194,8 @@ typedef struct {
   int t_cols_flux;   /* columns per block of the column pass with the Burgers step: 8, 16 */
   int t_cols_plain;  /* columns per block of the taper-only column pass: 8, 16 */
   int t_cols_stats;  /* columns per block of the column pass closing a step: 8, 16 */
-  int xy_clusters;   /* cap on resident clusters of the L2-exchange plane kernel: 0..32 */
-  int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..32 */
+  int xy_clusters;   /* cap on resident CTA groups (clusters) of the L2-exchange plane kernel: 0..64 */
+  int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..64 */
   int xy_sync;       /* group barrier of those kernels: 1 thread-block cluster, 2 counter
                       * barrier in a cooperative launch (plans in a batch use 1) */
 } asg_tuning;

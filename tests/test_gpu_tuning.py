@@ -122,7 +122,7 @@ def test_autotune_picks_a_supported_shape_and_keeps_the_result():
         ref = _run(plan, u0, dz)
         chosen = plan.autotune(u0, dz, steps=2)
         assert chosen["t_cols_flux"] in (8, 16) and chosen["t_cols_plain"] in (8, 16)
-        assert 0 <= chosen["xy_clusters"] <= 32 and 0 <= chosen["xy_clusters_closing"] <= 32
+        assert 0 <= chosen["xy_clusters"] <= 64 and 0 <= chosen["xy_clusters_closing"] <= 64
         assert solver.TUNING_CACHE[plan.tuning_key] == chosen
         out = _run(plan, u0, dz)
         for k, a, b in zip(KEYS, ref, out):
