@@ -395,12 +395,10 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   }
   if (!p->xyfast) {
     p->G = 1;
-    if (asg_xy_generic_smem(X, Y) > 200 * 1024)
-      return fail(ASG_ERR_SHAPE,
-                  "grid %dx%d: no fast plane transform (needs nX = 32*G, G in "
-                  "{1,2,3,4,6,8,12,16}, nY in {64,96,128,192,256,384,512}) and the plane is too "
-                  "large for the generic in-shared-memory transform",
-                  X, Y);
+    // planes larger than one CTA's shared memory take the generic row/column
+    // passes over HBM (their column pass holds whole columns: nX <= 1024)
+    if (asg_xy_generic_smem(X, Y) > ASG_XY_GENERIC_MAX_SMEM && X > 1024)
+      return fail(ASG_ERR_SHAPE, "grid %dx%d: nX > 1024 without a fast plane transform", X, Y);
   }
   if (!p->tfast && asg_t_generic_smem(T) > 200 * 1024)
     return fail(ASG_ERR_SHAPE, "nT=%d too long for the generic column transform", T);
@@ -487,7 +485,8 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   // ---- device buffers ----
   const size_t nspec = (size_t)p->F * p->ncols;
   CKS(dalloc(&p->spec, nspec));
-  if (p->split && !p->l2) CKS(dalloc(&p->spec2, nspec));
+  const bool big = !p->xyfast && asg_xy_generic_smem(X, Y) > ASG_XY_GENERIC_MAX_SMEM;
+  if ((p->split && !p->l2) || big) CKS(dalloc(&p->spec2, nspec));
   for (int q = 0; q < p->F; ++q)
     if (2 * p->h_f_of_plane[q] == T) p->nyq_plane = q;
   if (p->l2 && p->nyq_plane >= 0) CKS(dalloc(&p->nyq_tmp, (size_t)X * Y));
@@ -904,6 +903,7 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.coop = xy_sync_of(p) == 2 ? 1 : 0;
   x.grp_cnt = p->grp_cnt;
   x.grp_skew = p->barrier_skew;
+  x.spec_tmp = p->spec2;
   x.skip_plane = -1;
   return x;
 }

@@ -100,6 +100,7 @@ struct XYParams {
                            //    counters in grp_cnt instead of thread-block clusters
   unsigned* grp_cnt;       // [l2_max_clusters] arrival counters (zeroed by the launcher)
   unsigned grp_skew;       // added to every barrier target (test hook: 0 in normal runs)
+  float2* spec_tmp;        // [planes][X][Y] work spectrum of the large generic planes
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
 };
 
@@ -114,6 +115,9 @@ bool asg_xy_split_supported(int X, int Y, int* G_out);
 int asg_launch_epilogue_pass(const XYParams& p, const float2* src, float2* dst, int split,
                              cudaStream_t st);
 size_t asg_xy_generic_smem(int X, int Y);
+// planes whose generic transform needs more shared memory than this run as
+// row and column passes over HBM through XYParams::spec_tmp (nX <= 1024)
+constexpr size_t ASG_XY_GENERIC_MAX_SMEM = 200 * 1024;
 int asg_launch_xy(const XYParams& p, bool fast, const GenPlan& plx, const GenPlan& ply,
                   cudaStream_t st);
 

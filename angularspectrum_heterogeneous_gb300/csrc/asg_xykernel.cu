@@ -596,6 +596,135 @@ __global__ void __launch_bounds__(256) xy_generic(XYParams p, GenPlan plx, GenPl
 }
 
 // ---------------------------------------------------------------------------
+// Generic kernels for planes too large for one CTA's shared memory (the odd
+// sizes of the reference's validation scripts: 257 x 257, 365 x 365, ...):
+// the plane transform runs as three passes over HBM, rows (y transform) of
+// RB rows per CTA, then columns (x transform, multiplier, inverse x
+// transform) of CB columns per CTA, then rows again (inverse y transform),
+// each line a mixed-radix Stockham FFT in shared memory.  The boundary and
+// screen epilogue, when the stage has one, follows as the tiled epilogue pass.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) xy_big_rows(XYParams p, GenPlan ply, const float2* src,
+                                                   float2* dst, int inverse, int rb) {
+  const int X = p.X, Y = p.Y;
+  extern __shared__ float4 smraw[];
+  float2* A = reinterpret_cast<float2*>(smraw);
+  float2* B = A + rb * Y;
+  float2* twY = B + rb * Y;
+  const int plane = blockIdx.y, x0 = blockIdx.x * rb;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  if (xy_should_skip(p)) return;
+  // (planes of bins 0 and nT/2 of the analytic-signal propagator are zeroed
+  // by the column pass; the inverse row pass carries the zeros to dst)
+  const int nr = min(rb, X - x0);
+  for (int i = tid; i < Y; i += nthr) twY[i] = p.twY[i];
+  const float2* s = src + ((size_t)plane * X + x0) * Y;
+  for (int i = tid; i < nr * Y; i += nthr) A[i] = s[i];
+  __syncthreads();
+  float2* r = inverse ? gen_fft<true>(A, B, nr, Y, 1, ply, twY) : gen_fft<false>(A, B, nr, Y, 1, ply, twY);
+  float2* d = dst + ((size_t)plane * X + x0) * Y;
+  for (int i = tid; i < nr * Y; i += nthr) d[i] = r[i];
+}
+
+__global__ void __launch_bounds__(256) xy_big_cols(XYParams p, GenPlan plx, float2* buf, int cb) {
+  const int X = p.X, Y = p.Y;
+  extern __shared__ float4 smraw[];
+  float2* A = reinterpret_cast<float2*>(smraw);  // [c][x]: one line per column
+  float2* B = A + cb * X;
+  float2* twX = B + cb * X;
+  __shared__ float red[2][8];
+  const int plane = blockIdx.y, y0 = blockIdx.x * cb;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  if (xy_should_skip(p)) return;
+  const int nc = min(cb, Y - y0);
+  float2* g = buf + (size_t)plane * X * Y + y0;
+  if (p.zero_dc_nyq && is_dc_or_nyq(p.f_of_plane[plane], p.nT)) {
+    for (int i = tid; i < X * nc; i += nthr) {
+      const int x = i / nc, c = i - x * nc;
+      g[(size_t)x * Y + c] = make_float2(0.f, 0.f);
+    }
+    return;
+  }
+  for (int i = tid; i < X; i += nthr) twX[i] = p.twX[i];
+  for (int i = tid; i < X * nc; i += nthr) {
+    const int x = i / nc, c = i - x * nc;
+    A[c * X + x] = g[(size_t)x * Y + c];
+  }
+  __syncthreads();
+  float2* r = gen_fft<false>(A, B, nc, X, 1, plx, twX);
+  float psum = 0.f, pden = 0.f;
+  const float nrm = 1.0f / ((float)X * (float)Y);
+  for (int i = tid; i < X * nc; i += nthr) {
+    const int c = i / X, x = i - c * X;
+    const size_t ti = ((size_t)plane * p.ncx + p.cls_x[x]) * p.ncy + p.cls_y[y0 + c];
+    if (p.power_only) {
+      const float o = p.obl_table[ti];
+      const float P = r[i].x * r[i].x + r[i].y * r[i].y;
+      psum = fmaf(P, o, psum);
+      pden += (o > 0.f) ? P : 0.f;
+    } else if (p.table != nullptr) {
+      r[i] = cmul(r[i], p.table[ti]);
+    } else {
+      r[i] = cscale(r[i], nrm);
+    }
+  }
+  if (p.power_only) {
+    psum = warp_sum(psum);
+    pden = warp_sum(pden);
+    if ((tid & 31) == 0) {
+      red[0][tid >> 5] = psum;
+      red[1][tid >> 5] = pden;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double a = 0.0, b = 0.0;
+      for (int w = 0; w < nthr / 32; ++w) {
+        a += (double)red[0][w];
+        b += (double)red[1][w];
+      }
+      atomicAdd(p.power_acc, a);
+      atomicAdd(p.power_acc + 1, b);
+    }
+    return;
+  }
+  __syncthreads();
+  float2* o = (r == A) ? B : A;
+  float2* r2 = gen_fft<true>(r, o, nc, X, 1, plx, twX);
+  for (int i = tid; i < X * nc; i += nthr) {
+    const int x = i / nc, c = i - x * nc;
+    g[(size_t)x * Y + c] = r2[c * X + x];
+  }
+}
+
+size_t asg_xy_big_rows(int X, int Y) { return (size_t)(4096 / Y > 0 ? 4096 / Y : 1); }
+size_t asg_xy_big_cols(int X, int Y) { return (size_t)(4096 / X > 0 ? 4096 / X : 1); }
+
+// rows forward (spec -> tmp), columns (tmp), rows inverse (tmp -> spec, or
+// tmp -> tmp and the epilogue pass tmp -> spec); the power reduction stops
+// after the columns and leaves spec untouched
+static int launch_xy_big(const XYParams& p, const GenPlan& plx, const GenPlan& ply,
+                         cudaStream_t st) {
+  if (p.spec_tmp == nullptr) return ASG_ERR_STATE;
+  const int rb = (int)asg_xy_big_rows(p.X, p.Y), cb = (int)asg_xy_big_cols(p.X, p.Y);
+  const size_t smr = (size_t)(2 * rb * p.Y + p.Y) * sizeof(float2);
+  const size_t smc = (size_t)(2 * cb * p.X + p.X) * sizeof(float2);
+  if (cudaFuncSetAttribute(xy_big_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(xy_big_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc) !=
+          cudaSuccess)
+    return ASG_ERR_CUDA;
+  const dim3 gr((p.X + rb - 1) / rb, p.nplanes), gc((p.Y + cb - 1) / cb, p.nplanes);
+  xy_big_rows<<<gr, 256, smr, st>>>(p, ply, p.spec, p.spec_tmp, 0, rb);
+  xy_big_cols<<<gc, 256, smc, st>>>(p, plx, p.spec_tmp, cb);
+  if (p.power_only) return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
+  const bool epi = p.epi != 0 || p.nscreens > 0;
+  xy_big_rows<<<gr, 256, smr, st>>>(p, ply, p.spec_tmp, epi ? p.spec_tmp : p.spec, 1, rb);
+  if (cudaPeekAtLastError() != cudaSuccess) return ASG_ERR_CUDA;
+  if (epi) return asg_launch_epilogue_pass(p, p.spec_tmp, p.spec, 0, st);
+  return ASG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // (x, y, omega) epilogue as its own pass over 32 x 32 tiles with a one-cell
 // halo.  Input: the closing stage's output, either whole planes or the
 // half-plane form (rows x < X/2 hold a, rows x >= X/2 hold b, and
@@ -826,6 +955,7 @@ int asg_launch_xy(const XYParams& p, bool fast, const GenPlan& plx, const GenPla
     return ASG_ERR_SHAPE;
   }
   const size_t smem = asg_xy_generic_smem(p.X, p.Y);
+  if (smem > ASG_XY_GENERIC_MAX_SMEM) return launch_xy_big(p, plx, ply, st);
   if (cudaFuncSetAttribute(xy_generic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return ASG_ERR_CUDA;

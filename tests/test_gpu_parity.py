@@ -155,6 +155,14 @@ FAST_CASES = {
     "kt_fw_sa_64x128": ((64, 128, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                              useSuperAbsorbing=True), 8e6, 10),
     "lie_water_96": ((96, 96, 192), dict(useSplitStep=False, alpha0=-1.0), 3e6, 8),
+    # planes too large for one CTA's shared memory: generic row and column passes
+    # over HBM, the epilogue pass, screens and sources; and the power reduction
+    "big_odd_kt_fw_sa": ((121, 119, 64), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
+                                              useSuperAbsorbing=True), 4e6, 4,
+                         dict(zs=[3.0e-4, 6.0e-4], amp=[False, True]),
+                         dict(zs=[5.0e-4])),
+    "big_odd_obl": ((129, 127, 48), dict(fluxScheme="kt", useNonlinearityObliquity=True),
+                    4e6, 3),
     # groups of 8 CTAs: plane kernels in a cooperative launch with counter barriers,
     # with the beam-obliquity power pass (its extra barrier) in the second case
     "kt_fw_sa_256_coop": ((256, 256, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
