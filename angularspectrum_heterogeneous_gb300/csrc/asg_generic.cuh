@@ -34,23 +34,27 @@ ASG_DEV void gen_butterfly_reg(const float2* s, float2* d, int es, int j, int nb
   for (int r = 0; r < R; ++r) d[(db + r * Ns) * es] = v[r];
 }
 
+// Output k of a direct radix-R butterfly (any prime factor).  The twiddle of
+// input r is W_n^e with e = (r twstep + ((r k) mod R) nb) mod n
+// = r (twstep + k nb) mod n (since R nb = n), stepped incrementally.
 template <bool INV>
 ASG_DEV void gen_butterfly_direct(const float2* s, float2* d, int es, int j, int nb, int Ns,
-                                  int twstep, int R, int n, const float2* twn) {
+                                  int twstep, int R, int n, const float2* twn, int k) {
   const int jm = j % Ns;
   const int db = (j / Ns) * Ns * R + jm;
-  for (int k = 0; k < R; ++k) {
-    float accx = 0.f, accy = 0.f;
-    for (int r = 0; r < R; ++r) {
-      float2 x = s[(j + r * nb) * es];
-      int e = (int)(((long long)r * twstep + (long long)((r * k) % R) * nb) % n);
-      float2 w = twn[e];
-      float2 y = INV ? cmulc(x, w) : cmul(x, w);
-      accx += y.x;
-      accy += y.y;
-    }
-    d[(db + k * Ns) * es] = make_float2(accx, accy);
+  const int inc = (int)(((long long)twstep + (long long)k * nb) % n);
+  float accx = 0.f, accy = 0.f;
+  int e = 0;
+  for (int r = 0; r < R; ++r) {
+    float2 x = s[(j + r * nb) * es];
+    float2 w = twn[e];
+    float2 y = INV ? cmulc(x, w) : cmul(x, w);
+    accx += y.x;
+    accy += y.y;
+    e += inc;
+    if (e >= n) e -= n;
   }
+  d[(db + k * Ns) * es] = make_float2(accx, accy);
 }
 
 // FFT of `nlines` lines: element e of line l at buf[l*ls + e*es].  Runs over
@@ -65,9 +69,12 @@ ASG_DEV float2* gen_fft(float2* buf0, float2* buf1, int nlines, int ls, int es, 
   for (int p = 0; p < pl.nrad; ++p) {
     const int R = pl.rad[p];
     const int nb = n / R;
-    const int total = nlines * nb;
+    // direct butterflies spread their R outputs over threads
+    const int per = (R == 2 || R == 3 || R == 4 || R == 8) ? 1 : R;
+    const int total = nlines * nb * per;
     for (int it = threadIdx.x; it < total; it += blockDim.x) {
-      const int l = it / nb, j = it - (it / nb) * nb;
+      const int q = it / per, k = it - q * per;
+      const int l = q / nb, j = q - l * nb;
       const float2* s = src + (size_t)l * ls;
       float2* d = dst + (size_t)l * ls;
       const int twstep = (j % Ns) * (n / (Ns * R));
@@ -76,7 +83,7 @@ ASG_DEV float2* gen_fft(float2* buf0, float2* buf1, int nlines, int ls, int es, 
         case 3: gen_butterfly_reg<3, INV>(s, d, es, j, nb, Ns, twstep, n, twn); break;
         case 4: gen_butterfly_reg<4, INV>(s, d, es, j, nb, Ns, twstep, n, twn); break;
         case 8: gen_butterfly_reg<8, INV>(s, d, es, j, nb, Ns, twstep, n, twn); break;
-        default: gen_butterfly_direct<INV>(s, d, es, j, nb, Ns, twstep, R, n, twn); break;
+        default: gen_butterfly_direct<INV>(s, d, es, j, nb, Ns, twstep, R, n, twn, k); break;
       }
     }
     __syncthreads();

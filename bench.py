@@ -45,10 +45,12 @@ def set_grid(nx, ny, nt):
     NX, NY, NT = nx, ny, nt
     V = NX * NY * NT
 B_ALG = 48.0  # algorithmic bytes per voxel-step of the Strang path (3 stages x 2 sweeps x 8 B)
-# DRAM bytes (read + write) per voxel of one launch of each pass, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the workload's
-# options on a 256 x 256 x 1024 grid; the traffic scales with the voxel count.
-DRAM_BYTES_PER_VOXEL = {"xy_A": 8.254, "xy_B": 8.256, "xy_C": 8.394, "t_nonlin": 7.198,
+# DRAM bytes (read + write) per voxel of one launch of each pass, from ncu
+# captures (dram__bytes_read.sum + dram__bytes_write.sum) of the workload's
+# options: the plane passes on a 512 x 512 x 256 grid (the workload's planes),
+# the column passes on 256 x 256 x 1024 (its columns); the traffic scales with
+# the voxel count.
+DRAM_BYTES_PER_VOXEL = {"xy_A": 8.448, "xy_B": 8.477, "xy_C": 11.570, "t_nonlin": 7.198,
                         "t_mid": 7.195, "t_end": 7.329}
 B_SWEEP = 8.0  # algorithmic bytes per voxel of one pass (read 4 + write 4)
 METRIC = "voxel-steps/s"
@@ -281,7 +283,8 @@ def run_gpu_arm(args):
                          "frac": achieved / peak,
                          "traffic": (DRAM_BYTES_PER_VOXEL[dom] * V
                                      if dom in DRAM_BYTES_PER_VOXEL else None),
-                         "traffic_source": "ncu dram bytes per voxel at 256x256x1024, "
+                         "traffic_source": "ncu dram bytes per voxel (plane passes at "
+                                           "512x512x256, column passes at 256x256x1024), "
                                            "scaled to the grid", "kernel": dom,
                          "peak_source": peak_kind,
                          "step_frac": value * B_ALG / 1e9 / peak},
