@@ -1,0 +1,306 @@
+"""Known-answer cases of the reference's validation scripts, restated for the
+solve API (plain numpy: case inputs and the metrics computed from outputs).
+
+Each case gives the solver keyword arguments and initial field of one of the
+reference's checks, and a metric function of the solve outputs.  The tests
+run them through the GPU path (and the oracle where that is cheap) and
+compare with the reference's published figures:
+
+  dc_*          validate_dc_invariance.py:27-94  (DC growth <= 1, peak spread <= 5 %)
+  reflection_*  validate_boundaries.py:92-168    (boundary/centre intensity ratios,
+                                                  read off test2_reflection_bar.png)
+  order_*       validate_solver.py:467-551       (isolated Burgers-step order:
+                                                  Rusanov ~1.05, KT ~1.90)
+  convergence_* validate_solver.py:345-461       (pairwise Strang/Lie convergence)
+  attenuation_* validate_solver.py:795-960       (power law and Kramers-Kronig)
+  baffled_*     validate_analytical.py:126-278   (Rayleigh/Fresnel on-axis, RMS 0.0861)
+  focused_*     validate_analytical.py:284-458   (paraxial focus, RMS 0.0645 / 0.0024)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# figures the reference publishes for these cases (titles of its result plots,
+# README and the bar chart of validate_boundaries.py)
+PUBLISHED = {
+    "reflection": {"quadratic": 0.0183, "wendland": 0.0135, "freq_weighted": 0.0094,
+                   "all_combined": 0.0075},
+    "order": {"rusanov": 1.05, "kt": 1.90},
+    "convergence": {"split_kt_err32": 8.3e-4, "split_kt_err16": 2.2e-4},
+    "baffled_onaxis_rms": 0.0861,
+    "focused_onaxis_rms": 0.0645,
+    "focused_lateral_rms": 0.0024,
+}
+
+
+# ---------------------------------------------------------------------------
+# DC-bin invariance: a pulse uniform in (x, y), 64 plain diffraction steps
+# ---------------------------------------------------------------------------
+def dc_case(nT, nX=32, nY=32, f0=1.0e6, c0=1500.0, n_cycles=3, n_steps=64):
+    lam = c0 / f0
+    dX = lam / 8
+    dZ = lam / 4
+    dT = 1.0 / (f0 * 16)
+    t = np.arange(nT) * dT
+    env = np.exp(-((t - n_cycles / f0 * 0.5) / (n_cycles / f0 / 4)) ** 2)
+    pulse = (np.sin(2 * np.pi * f0 * t) * env).astype(np.float32)
+    u0 = np.ascontiguousarray(np.broadcast_to(pulse[None, None, :], (nX, nY, nT)))
+    # linear, lossless, no taper, no adaptive filter, sequential splitting:
+    # every step is the diffraction operator alone (plus identity operators)
+    kw = dict(dX=dX, dY=dX, dT=dT, c0=c0, rho0=1000.0, beta=0.0, alpha0=0.0, f0=f0,
+              propDist=n_steps * dZ, dZmin=dZ, useSplitStep=False, useAdaptiveFiltering=False,
+              useBoundaryLayer=False, useTVD=False)
+    return u0, kw
+
+
+def dc_metrics(u0, field):
+    """(peak |p|, DC growth = max |DC bin| out / in)."""
+    src = np.abs(np.fft.fft(u0.astype(np.float64), axis=2)[..., 0]).max()
+    out = np.abs(np.fft.fft(np.asarray(field, np.float64), axis=2)[..., 0]).max()
+    return float(np.abs(field).max()), float(out / max(src, 1e-30))
+
+
+# ---------------------------------------------------------------------------
+# rectangular-aperture pulse of validate_solver.py / validate_boundaries.py
+# ---------------------------------------------------------------------------
+def aperture_pulse(nX, nY, nT, dX, dT, f0, p0, wX, wY, ncycles=1.5, dur=2):
+    x = np.arange(nX) * dX - (nX - 1) * dX / 2
+    y = np.arange(nY) * dX - (nY - 1) * dX / 2
+    t = np.arange(nT) * dT
+    t = t - t.mean()
+    w0 = 2 * np.pi * f0
+    ap = ((np.abs(x)[:, None] <= wX / 2) & (np.abs(y)[None, :] <= wY / 2)).astype(np.float64)
+    sig = np.exp(-(1.05 * t * w0 / (ncycles * np.pi)) ** (2 * dur)) * np.sin(t * w0) * p0
+    return (ap[:, :, None] * sig[None, None, :]).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# boundary reflection: 81 x 81 x 101 wide aperture toward the edges, 3 cm
+# ---------------------------------------------------------------------------
+REFLECTION_CONFIGS = {
+    "quadratic": dict(boundaryProfile="quadratic", useFreqWeightedBoundary=False,
+                      useSuperAbsorbing=False),
+    "wendland": dict(boundaryProfile="wendland", useFreqWeightedBoundary=False,
+                     useSuperAbsorbing=False),
+    "freq_weighted": dict(boundaryProfile="wendland", useFreqWeightedBoundary=True,
+                          useSuperAbsorbing=False),
+    "all_combined": dict(boundaryProfile="wendland", useFreqWeightedBoundary=True,
+                         useSuperAbsorbing=True, superAbsorbingStrength=0.5),
+}
+
+
+def reflection_case(name):
+    f0, c0 = 3e6, 1500.0
+    dX = c0 / f0 / 5
+    dT = dX / (5 * c0)
+    u0 = aperture_pulse(81, 81, 101, dX, dT, f0, 1e3, 8e-3, 8e-3)
+    kw = dict(dX=dX, dY=dX, dT=dT, c0=c0, rho0=1000.0, beta=0.0, alpha0=-1.0, f0=f0,
+              propDist=3e-2, boundaryFactor=0.15, useSplitStep=True,
+              useAdaptiveFiltering=False, useTVD=False, dZmin=4 * dX,
+              **REFLECTION_CONFIGS[name])
+    return u0, kw
+
+
+def reflection_ratio(pI):
+    """Intensity in the 15 % edge bands over the centre, last plane."""
+    last = np.asarray(pI[:, :, -1], np.float64)
+    nX, nY = last.shape
+    b = int(nX * 0.15)
+    c = slice(b, nX - b)
+    edge = last[:b].sum() + last[-b:].sum() + last[c, :b].sum() + last[c, -b:].sum()
+    centre = last[c, c].sum()
+    return float(edge / centre) if centre > 0 else 0.0
+
+
+# ---------------------------------------------------------------------------
+# isolated Burgers step order on one 801-sample column
+# ---------------------------------------------------------------------------
+ORDER_Z = 0.03
+ORDER_DZ = [ORDER_Z / 32, ORDER_Z / 64, ORDER_Z / 128, ORDER_Z / 256, ORDER_Z / 512]
+ORDER_REF_DZ = ORDER_Z / 4096
+
+
+def order_column():
+    """(u0 float32 (801,), dT, N)."""
+    t = np.linspace(-1.0, 1.0, 801)
+    u0 = 1.5 * np.exp(-(t / 0.22) ** 2) * np.sin(2 * np.pi * 4 * t)
+    u0[[0, -1]] = 0.0
+    return u0.astype(np.float32), float(t[1] - t[0]), 1.0
+
+
+def order_rate(finals, ref):
+    """Order from the three coarsest steps: slope of log RMS error vs log dZ."""
+    err = [float(np.sqrt(np.mean((np.asarray(u, np.float64) - ref) ** 2))) for u in finals]
+    return float(np.polyfit(np.log(ORDER_DZ[:3]), np.log(err[:3]), 1)[0]), err
+
+
+# ---------------------------------------------------------------------------
+# pairwise convergence of the full march (51 x 51 x 401, 3 MPa, 15 mm)
+# ---------------------------------------------------------------------------
+CONV_CONFIGS = {
+    "sequential": dict(useSplitStep=False, fluxScheme="rusanov"),
+    "split_rusanov": dict(useSplitStep=True, fluxScheme="rusanov"),
+    "split_kt": dict(useSplitStep=True, fluxScheme="kt"),
+}
+CONV_STEPS = [32, 16, 8, 4, 2]  # dZ / dX
+
+
+def convergence_case(name, dz_over_dx):
+    f0, c0 = 3e6, 1500.0
+    dX = c0 / f0 / 5
+    dT = dX / (5 * c0)
+    u0 = aperture_pulse(51, 51, 401, dX, dT, f0, 3.0e6, 5e-3, 5e-3)
+    kw = dict(dX=dX, dY=dX, dT=dT, c0=c0, rho0=1000.0, beta=3.5, alpha0=0.1, attenPow=1.0,
+              f0=f0, propDist=1.5e-2, boundaryFactor=0.15, useBoundaryLayer=False,
+              useAdaptiveFiltering=False, useTVD=False, stabilityThreshold=1e9,
+              stabilityRecoveryFactor=0.15, dZmin=dz_over_dx * dX, **CONV_CONFIGS[name])
+    return u0, kw
+
+
+def pair_errors(traces):
+    """RMS(coarse - fine) / RMS(fine) of consecutive step sizes' centre traces."""
+    out = []
+    for a, b in zip(traces[:-1], traces[1:]):
+        a = np.asarray(a, np.float64)
+        b = np.asarray(b, np.float64)
+        out.append(float(np.sqrt(np.mean((a - b) ** 2)) / (np.sqrt(np.mean(b ** 2)) + 1e-30)))
+    return out
+
+
+def pair_rate(errs):
+    x = np.log(np.array(CONV_STEPS[:-1], np.float64)[:3])
+    return float(np.polyfit(x, np.log(np.array(errs[:3])), 1)[0])
+
+
+# ---------------------------------------------------------------------------
+# attenuation and Kramers-Kronig dispersion of a broadband plane pulse
+# ---------------------------------------------------------------------------
+def attenuation_case():
+    f0, c0 = 3e6, 1540.0
+    dX = c0 / f0 / 3
+    dT = 1.0 / 60e6
+    nT = 1001
+    t = np.arange(nT) * dT
+    t = t - t.mean()
+    sig = np.exp(-0.5 * (t / (0.15 / f0)) ** 2) * np.sin(2 * np.pi * f0 * t)
+    u0 = np.ascontiguousarray(np.broadcast_to(sig[None, None, :], (5, 5, nT))).astype(np.float32)
+    kw = dict(dX=dX, dY=dX, dT=dT, c0=c0, rho0=1000.0, beta=0.0, alpha0=0.5, attenPow=1.0,
+              f0=f0, propDist=20e-3, boundaryFactor=0.0, useBoundaryLayer=False,
+              useSplitStep=True, fluxScheme="kt", useAdaptiveFiltering=False, useTVD=False,
+              stabilityThreshold=0.2, stabilityRecoveryFactor=0.15, dZmin=dX)
+    return u0, kw
+
+
+def attenuation_metrics(u0, field, zaxis, kw):
+    """(attenuation RMS error in dB/cm, phase-velocity RMS error in m/s), both
+    over 1-5 MHz against the power law and its Kramers-Kronig velocity."""
+    nX, nY, nT = u0.shape
+    dT, c0, f0, a0 = kw["dT"], kw["c0"], kw["f0"], kw["alpha0"]
+    z = float(zaxis[-1])
+    Fi = np.fft.rfft(np.asarray(u0[nX // 2, nY // 2], np.float64))
+    Fo = np.fft.rfft(np.asarray(field[nX // 2, nY // 2], np.float64))
+    f = np.fft.rfftfreq(nT, dT)
+    ok = np.abs(Fi) > np.abs(Fi).max() * 1e-3
+    a_db = -np.log(np.abs(Fo[ok]) / np.abs(Fi[ok]) + 1e-30) / z * 20 * np.log10(np.e) / 1e2
+    ph = np.unwrap(np.angle(Fo[ok] / Fi[ok]))
+    fv = f[ok]
+    c_meas = 1.0 / (1.0 / c0 + (-ph / z) / (2 * np.pi * fv + 1e-30))
+    conv = a0 / 1e6 * 1e2 / (20 * np.log10(np.e))
+    astar0 = (-2 * conv / (2 * np.pi) / np.pi) * (np.log(2 * np.pi * np.maximum(fv, 1.0))
+                                                  - np.log(2 * np.pi * f0))
+    c_kk = 1.0 / (1.0 / c0 + 2 * np.pi * astar0 * fv / (2 * np.pi * fv))
+    band = (fv >= 1e6) & (fv <= 5e6)
+    a_err = a_db - a0 * fv / 1e6
+    return (float(np.sqrt(np.mean(a_err[band] ** 2))),
+            float(np.sqrt(np.mean((c_meas[band] - c_kk[band]) ** 2))))
+
+
+# ---------------------------------------------------------------------------
+# circular pistons against paraxial analytic solutions (linear, lossless)
+# ---------------------------------------------------------------------------
+def _piston_grid(nX, nT, f0, c0):
+    lam = c0 / f0
+    dX = lam / 5
+    dT = dX / (5 * c0)
+    x = np.arange(nX) * dX - (nX - 1) * dX / 2
+    t = np.arange(nT) * dT - (nT - 1) * dT / 2
+    return lam, dX, dT, x, t
+
+
+def _piston_kw(dX, dT, c0, f0, prop, dZ):
+    # linear, lossless, no taper and no adaptive filter: each step is the plain
+    # diffraction operator of the reference's analytic tests
+    return dict(dX=dX, dY=dX, dT=dT, c0=c0, rho0=1000.0, beta=0.0, alpha0=0.0, f0=f0,
+                propDist=prop, dZmin=dZ, useSplitStep=False, useAdaptiveFiltering=False,
+                useBoundaryLayer=False, useTVD=False)
+
+
+def baffled_case(a_lambda=6.0, nX=257, nT=721):
+    f0, c0, p0 = 4e6, 1500.0, 0.3e6
+    lam, dX, dT, x, t = _piston_grid(nX, nT, f0, c0)
+    a = a_lambda * lam
+    w0 = 2 * np.pi * f0
+    sig = (np.exp(-(1.05 * t * w0 / (3.0 * np.pi)) ** 4) * np.sin(t * w0) * p0).astype(np.float32)
+    ap = ((x[:, None] ** 2 + x[None, :] ** 2) <= a ** 2).astype(np.float32)
+    u0 = ap[:, :, None] * sig[None, None, :]
+    return u0, _piston_kw(dX, dT, c0, f0, 0.05, 8 * dX), dict(a=a, lam=lam, p0=p0, x=x)
+
+
+def baffled_metrics(pax, pI, zaxis, g):
+    """(on-axis RMS of the normalised |p| vs Rayleigh/Fresnel, far-field
+    lateral RMS vs (2 J1(u)/u)^2)."""
+    from scipy.special import j1
+    k0 = 2 * np.pi / g["lam"]
+    z = np.asarray(zaxis, np.float64)
+    num = np.abs(np.asarray(pax, np.float64)).max(axis=0)
+    ana = np.abs(-g["p0"] * (np.exp(1j * k0 * g["a"] ** 2 / (2 * z)) - 1))
+    rms = np.sqrt(np.mean((num / num.max() - ana / ana.max()) ** 2))
+    zff = max(2 * g["a"] ** 2 / g["lam"], z[-1] * 0.9)
+    i = int(np.argmin(np.abs(z - zff)))
+    u = np.maximum(k0 * g["a"] * np.abs(g["x"]) / z[i], 1e-10)
+    model = (2 * j1(u) / u) ** 2
+    model /= model.max()
+    lat = np.asarray(pI[:, pI.shape[1] // 2, i], np.float64)
+    lat /= lat.max() + 1e-30
+    return float(rms), float(np.sqrt(np.mean((lat - model) ** 2)))
+
+
+def focused_case(nX=257, nT=601):
+    f0, c0, p0 = 4e6, 1500.0, 0.3e6
+    lam, dX, dT, x, t = _piston_grid(nX, nT, f0, c0)
+    a, F = 8 * lam, 20e-3
+    w0 = 2 * np.pi * f0
+    sig = (np.exp(-(1.05 * t * w0 / (4.0 * np.pi)) ** 4) * np.sin(t * w0) * p0).astype(np.float32)
+    r2 = x[:, None] ** 2 + x[None, :] ** 2
+    shift = np.round((F - np.sqrt(F ** 2 + r2)) / c0 / dT).astype(np.int64)
+    u0 = np.zeros((nX, nX, nT), np.float32)
+    ix, iy = np.nonzero(r2 <= a ** 2)
+    # integer-sample delays: the aperture pixel's pulse rolled by its delay
+    idx = (np.arange(nT)[None, :] - shift[ix, iy][:, None]) % nT
+    u0[ix, iy, :] = sig[idx]
+    return u0, _piston_kw(dX, dT, c0, f0, 0.05, 2 * dX), dict(a=a, F=F, lam=lam, p0=p0, x=x,
+                                                                 dZ=2 * dX)
+
+
+def focused_metrics(pax, pI, zaxis, g):
+    """(on-axis RMS of the normalised |p| vs the paraxial focused piston,
+    focal-plane lateral RMS vs (2 J1(u)/u)^2, |p(F)| error vs p0 pi a^2/(lam F))."""
+    from scipy.special import j1
+    k0 = 2 * np.pi / g["lam"]
+    a, F, p0 = g["a"], g["F"], g["p0"]
+    z = np.asarray(zaxis, np.float64)
+    num = np.abs(np.asarray(pax, np.float64)).max(axis=0)
+    arg = k0 * a ** 2 * (F - z) / (4.0 * F * np.maximum(z, 1e-9))
+    den = F - z
+    ana = 2.0 * p0 * np.abs(F / np.where(np.abs(den) < 1e-9, 1e-9, den)) * np.abs(np.sin(arg))
+    focal = p0 * np.pi * a ** 2 / (g["lam"] * F)
+    ana[np.abs(z - F) < 2 * g["dZ"]] = focal
+    iF = int(np.argmin(np.abs(z - F)))
+    rms = np.sqrt(np.mean((num / num.max() - ana / ana.max()) ** 2))
+    u = np.maximum(k0 * a * np.abs(g["x"]) / F, 1e-10)
+    model = (2 * j1(u) / u) ** 2
+    model /= model.max()
+    lat = np.asarray(pI[:, pI.shape[1] // 2, iF], np.float64)
+    lat /= lat.max() + 1e-30
+    return (float(rms), float(np.sqrt(np.mean((lat - model) ** 2))),
+            float(abs(num[iF] - focal) / focal))
