@@ -143,3 +143,35 @@ def test_focused_piston_paraxial():
     ora = ORACLE["focused"]
     assert abs(on - ora["onaxis_rms"]) <= 0.001, (on, ora)
     assert abs(fe - ora["focal_amp_err"]) <= 0.01, (fe, ora)
+
+
+def test_riemann_shock():
+    """validate_analytical.py test B restated for the column step: the KT step
+    against the exact Burgers shock, below the published errors of the
+    reference's first-order finite-volume KT (0.033 / 0.033 / 0.036) and equal
+    to the oracle's; the standard Rusanov step (twice the KT flux in the
+    reference) against the shock at speed 2."""
+    import torch
+    import oracle.asm_oracle as O
+    from angularspectrum_heterogeneous_gb300 import _lib
+    lib = _lib.load()
+    _, dT, _ = K.riemann_column()
+    stream = torch.cuda.current_stream()
+
+    def gpu_step(flux):
+        def step(u, dz):
+            a = torch.from_numpy(np.ascontiguousarray(u, np.float32)).cuda()
+            b = torch.empty_like(a)
+            _lib.check(lib.asg_flux_columns_device(
+                C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), 1, a.numel(), flux, 1.0, dz,
+                dT, 1.0, 0.0, 1, C.c_void_p(stream.cuda_stream)))
+            stream.synchronize()
+            return b.cpu().numpy()
+        return step
+
+    kt = K.riemann_errors(gpu_step(_lib.FLUX_KT))
+    ref = K.riemann_errors(lambda u, dz: np.asarray(O.flux_kt(u.reshape(1, 1, -1), 1.0, dz, dT))[0, 0])
+    assert all(e < p for e, p in zip(kt, K.RIEMANN_PUBLISHED_KT)), kt
+    assert all(abs(e - r) <= 0.02 * r for e, r in zip(kt, ref)), (kt, ref)
+    ru = K.riemann_errors(gpu_step(_lib.FLUX_RUSANOV), speed=2.0)
+    assert max(ru) < 0.045, ru

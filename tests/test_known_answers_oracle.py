@@ -68,3 +68,15 @@ def test_stored_metrics_match_published_figures():
     assert abs(FIX["baffled"]["onaxis_rms"] - K.PUBLISHED["baffled_onaxis_rms"]) <= 5e-4
     assert abs(FIX["focused"]["onaxis_rms"] - K.PUBLISHED["focused_onaxis_rms"]) <= 5e-4
     assert abs(FIX["focused"]["lateral_rms"] - K.PUBLISHED["focused_lateral_rms"]) <= 1e-4
+
+
+def test_riemann_shock():
+    """The KT step against the exact shock (below the published errors of the
+    reference's first-order finite-volume KT); the standard Rusanov step of
+    the reference carries twice the flux, so its shock runs at speed 2."""
+    _, dT, _ = K.riemann_column()
+    kt = K.riemann_errors(lambda u, dz: np.asarray(O.flux_kt(u.reshape(1, 1, -1), 1.0, dz, dT))[0, 0])
+    assert all(e < p for e, p in zip(kt, K.RIEMANN_PUBLISHED_KT)), kt
+    ru = K.riemann_errors(
+        lambda u, dz: np.asarray(O.flux_rusanov(u.reshape(1, 1, -1), 1.0, dz, dT))[0, 0], speed=2.0)
+    assert max(ru) < 0.045, ru
