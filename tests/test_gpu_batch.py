@@ -18,6 +18,9 @@ INSTANCES = [
     ((64, 64, 512), dict(fluxScheme="kt"), 6e6, 4.0, False),
     ((48, 40, 96), dict(useSplitStep=False, alpha0=-1.0), 1e6, 6.0, True),
     ((128, 128, 256), dict(fluxScheme="kt", useSuperAbsorbing=True), 5e5, 3.25, False),
+    # 512-wide planes: a cooperative launch alone, thread-block clusters in the batch
+    ((512, 512, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
+                           useSuperAbsorbing=True), 2e6, 3.0, False),
 ]
 
 
@@ -46,6 +49,13 @@ def test_batch_matches_single_runs_and_oracle():
         singles.append(angular_spectrum_solve(u0, prm, verbose=False))
     outs, ms = solve_batch(fields, params, return_timing=True)
     assert ms > 0
+    # the lone 512-wide plan ran as a cooperative launch
+    from angularspectrum_heterogeneous_gb300 import Plan
+    pl = Plan(fields[-1].shape, params[-1])
+    try:
+        assert pl.get_tuning()["xy_sync"] == 2
+    finally:
+        pl.close()
     for j, (a, b) in enumerate(zip(outs, singles)):
         for k, x, y in zip(KEYS, a, b):
             assert x.shape == y.shape, (j, k)
