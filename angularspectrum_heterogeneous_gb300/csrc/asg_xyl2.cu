@@ -1,17 +1,20 @@
 // Plane kernel with the x exchange through an L2-resident scratch.
 //
-// A thread-block cluster of G CTAs owns one (half-)plane of Xs x Y modes at a
-// time (persistent, planes strided by the cluster count):
+// A group of G CTAs owns one (half-)plane of Xs x Y modes at a time
+// (persistent, planes strided by the group count).  The group is a
+// thread-block cluster, or, for G >= 12, G consecutive CTAs of a cooperative
+// launch that meet at counter barriers in global memory (a 16-CTA cluster must
+// fit in one GPC, which leaves a quarter of the SMs idle):
 //   1. each CTA loads R rows (cp.async, prefetched during the previous
 //      plane), runs the forward y FFT in shared memory and writes the rows to
-//      the cluster's scratch buffer in global memory (it stays in L2);
-//   2. cluster barrier; each CTA takes Yc = Y/G y-columns of all Xs rows from
+//      the group's scratch buffer in global memory (it stays in L2);
+//   2. group barrier; each CTA takes Yc = Y/G y-columns of all Xs rows from
 //      the scratch, runs the forward x FFT, the per-mode multiplier and the
 //      inverse x FFT (the middle four-step stage, multiplier and its inverse
 //      never leave registers), and writes the columns back;
-//   3. cluster barrier; each CTA reads its rows back, runs the inverse y FFT
+//   3. group barrier; each CTA reads its rows back, runs the inverse y FFT
 //      and stores the rows to HBM.
-// One scratch half-plane per cluster suffices with two barriers per plane:
+// One scratch half-plane per group suffices with two barriers per plane:
 // stages 1 and 3 of a CTA touch only its own rows.  Shared memory holds either R rows
 // or Xs x Yc columns, both about 64 KB for 512 x 512 planes split in halves,
 // so two CTAs share an SM.
