@@ -370,8 +370,11 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
                            bool write_stats, float* skew = nullptr) {
   const int lane = threadIdx.x & 31;
   const unsigned mask = 0xffffffffu;
+  // the KT steps on the skewed copy take the taper on the way into it
+  const bool fuse_taper =
+      SKEWED && CH <= 32 && (op.flux == FLUX_KT_MC || op.flux == FLUX_KT_MINMOD);
   // 1) taper
-  if (op.abl_xy != nullptr) {
+  if (op.abl_xy != nullptr && !fuse_taper) {
     const float axy = op.abl_xy[c];
 #pragma unroll
     for (int i = 0; i < CH; ++i) {
@@ -392,9 +395,25 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
     if (op.flux == FLUX_RUSANOV || op.flux == FLUX_RUSANOV_TVD) {
       rusanov_column(col, nT, coef_rus, op.flux == FLUX_RUSANOV_TVD, op.beta_tvd, mask);
     } else {
+      if constexpr (CH <= 32 && SKEWED) {
+        // taper (when fused) and copy into the bank-conflict-free layout
+        const SkewColumn sk{skew};
+        const float axy = op.abl_xy != nullptr ? op.abl_xy[c] : 1.f;
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int t = lane + 32 * i;
+          if (t < nT) {
+            const float v = col.get(t);
+            sk.set(t, op.abl_xy != nullptr ? v * (axy * op.abl_t[t]) : v);
+          }
+        }
+        __syncwarp(mask);
+      }
       int nsub = 1;
       if (op.cfl_target > 0.f) {
-        float um = column_absmax(col, nT);
+        float um;
+        if constexpr (CH <= 32 && SKEWED) um = column_absmax(SkewColumn{skew}, nT);
+        else um = column_absmax(col, nT);
         float cfl = ndt * um * op.dz;
         if (!(cfl <= op.cfl_target || um < 1e-30f)) {
           float q = ceilf(cfl / op.cfl_target);
@@ -406,14 +425,8 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
       float dzs = op.dz / (float)nsub;
       if constexpr (CH <= 32 && SKEWED) {
         {
-          // sub-steps on a bank-conflict-free copy of the column
+          // sub-steps on the bank-conflict-free copy of the column
           const SkewColumn sk{skew};
-#pragma unroll
-          for (int i = 0; i < CH; ++i) {
-            const int t = lane + 32 * i;
-            if (t < nT) sk.set(t, col.get(t));
-          }
-          __syncwarp(mask);
           for (int k = 0; k < nsub; ++k) {
             if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(sk, nT, ndt, dzs, mask);
             else kt_column_step_chunk<CH, false>(sk, nT, ndt, dzs, mask);
