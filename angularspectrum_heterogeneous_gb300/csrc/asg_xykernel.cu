@@ -696,8 +696,9 @@ __global__ void __launch_bounds__(256) xy_big_cols(XYParams p, GenPlan plx, floa
   }
 }
 
-size_t asg_xy_big_rows(int X, int Y) { return (size_t)(4096 / Y > 0 ? 4096 / Y : 1); }
-size_t asg_xy_big_cols(int X, int Y) { return (size_t)(4096 / X > 0 ? 4096 / X : 1); }
+// lines per CTA of the row and column passes: about 4096 complex (two 32 KB
+// ping-pong buffers)
+static int big_lines_per_cta(int n) { return 4096 / n > 0 ? 4096 / n : 1; }
 
 // rows forward (spec -> tmp), columns (tmp), rows inverse (tmp -> spec, or
 // tmp -> tmp and the epilogue pass tmp -> spec); the power reduction stops
@@ -705,7 +706,7 @@ size_t asg_xy_big_cols(int X, int Y) { return (size_t)(4096 / X > 0 ? 4096 / X :
 static int launch_xy_big(const XYParams& p, const GenPlan& plx, const GenPlan& ply,
                          cudaStream_t st) {
   if (p.spec_tmp == nullptr) return ASG_ERR_STATE;
-  const int rb = (int)asg_xy_big_rows(p.X, p.Y), cb = (int)asg_xy_big_cols(p.X, p.Y);
+  const int rb = big_lines_per_cta(p.Y), cb = big_lines_per_cta(p.X);
   const size_t smr = (size_t)(2 * rb * p.Y + p.Y) * sizeof(float2);
   const size_t smc = (size_t)(2 * cb * p.X + p.X) * sizeof(float2);
   if (cudaFuncSetAttribute(xy_big_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr) !=
