@@ -73,7 +73,7 @@ def workload_field(grid=None):
 
 def config(extra=None):
     c = {"workload": "plain KT march, 512x512x1024 focused piston 2 MPa, f0 2 MHz, "
-                     "freq-weighted + super-absorbing, dZ 1e-4 m (configs[1])",
+                     "freq-weighted + super-absorbing, dZ 1e-4 m",
          "grid": [NX, NY, NT], "voxels": V, "l2": "field and spectrum (1 GiB each) exceed L2; "
                                                     "no flush needed", "parallelism": "1 GPU"}
     if extra:
@@ -384,7 +384,7 @@ def run_batch_arm(args):
             "data": "synthetic",
             "config": {"workload": f"batched KT march of {len(insts)} focused-piston instances, "
                                    "nX=nY in {128,192,256,384}, nT in {256,512,1024}, focus "
-                                   "30-70 mm, steering +-10 deg, peak 0.2-3 MPa (configs[3])",
+                                   "30-70 mm, steering +-10 deg, peak 0.2-3 MPa",
                        "voxels": vox, "kt_cfl_target": BATCH_CFL, "parallelism": "1 GPU"},
             "one_at_a_time": {"value": vox * args.steps / (seq_ms / 1e3),
                               "ms_per_step": seq_ms / args.steps},
@@ -461,7 +461,7 @@ def run_learned_arm(args):
             "data": "synthetic",
             "config": {"workload": "Burgers stage of the 512x512x1024 2 MPa piston field, 2 mm "
                                    "KT step; learned (coarse + network where >= 10 sub-cycles) vs "
-                                   "plain KT sub-cycled at CFL 0.01 (configs[4] shape)",
+                                   "plain KT sub-cycled at CFL 0.01, 512x512x1024 columns",
                        "columns": int(cols.shape[0]), "learned_columns": int(nl),
                        "train_steps": len(hist), "train_seconds": t_train,
                        "final_loss": float(np.mean(hist[-20:]))},
@@ -545,7 +545,7 @@ def run_hetero_arm(args):
                                    "f0 1 MHz, TIPS-like 8-element bowl (radius 46 mm, roc "
                                    "80 mm, inner 20.5 mm, focus 50 mm, 400 kPa) as compact "
                                    "source planes, synthetic skull shell screens at z 20-29 mm, "
-                                   "linear water, dZ = dX, propDist 80 mm (configs[2])",
+                                   "linear water, dZ = dX, propDist 80 mm",
                        "grid": list(u0.shape), "march_steps": nsteps,
                        "source_planes": len(planes), "screens": len(screens),
                        "source_columns": int(sum(pl.cols.size for _, pl in planes)),

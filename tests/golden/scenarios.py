@@ -191,10 +191,10 @@ BASE = dict(dX=2.5e-4, dY=2.5e-4, dT=4.0e-8, c0=C0, rho0=RHO0, beta=3.5, alpha0=
             attenPow=1.0, f0=2.0e6, dZmin=2.5e-4, propDist=2.0e-3)
 
 SOLVE_SCENARIOS = {
-    # configs[0] option set, downscaled: Strang + TVD Rusanov + Wendland
+    # options of the 128x128x256 CPU-runnable piston workload, downscaled: Strang + TVD Rusanov + Wendland
     "strang_tvd_wendland": dict(shape=(16, 16, 48), p0=4e6,
                                 kw=dict(fluxScheme="rusanov", boundaryProfile="wendland")),
-    # configs[1] option set: KT + freq-weighted + super-absorbing
+    # options of the 512x512x1024 piston workload: KT + freq-weighted + super-absorbing
     "strang_kt_fw_sa": dict(shape=(16, 14, 64), p0=8e6,
                             kw=dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                     useSuperAbsorbing=True, f0=2.0e6)),

@@ -60,7 +60,7 @@ def test_batch_matches_single_runs_and_oracle():
         for k, x, y in zip(KEYS, a, b):
             assert x.shape == y.shape, (j, k)
             assert np.array_equal(x, y), (j, k)
-    # instance 0 (configs[1] options) against the FP64 oracle
+    # instance 0 (the 512x512x1024 workload's options) against the FP64 oracle
     u0, kw, ex = _inputs(*INSTANCES[0][:4], INSTANCES[0][4], 7)
     ref = O.solve(u0, oracle_params(kw, ex), "fp64")
     for k, a, r in zip(KEYS, outs[0], ref):

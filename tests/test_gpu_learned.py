@@ -1,7 +1,7 @@
 """The learned KT step: trained on the GPU by the library's own kernels on
 (column, sub-cycled KT column) pairs that the plain solver generates, it
-gains over the coarse step it corrects; the plain KT kernel is its fallback
-and the judge of its error."""
+gains over the coarse step it corrects; the plain sub-cycled KT kernel is its
+fallback and the reference its error is measured against."""
 import numpy as np
 import pytest
 

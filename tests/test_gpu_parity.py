@@ -148,10 +148,10 @@ def test_solve_vs_reference_fixtures(lib, name):
 # full solves on the fast kernels against the oracle run live (FP64)
 # ---------------------------------------------------------------------------
 FAST_CASES = {
-    # configs[0] option set on a 64^2 x 128 grid
+    # options of the 128x128x256 piston workload on a 64^2 x 128 grid
     "tvd_wendland_64": ((64, 64, 128), dict(fluxScheme="rusanov", boundaryProfile="wendland"),
                         4e6, 12),
-    # configs[1] option set: KT + freq-weighted + super-absorbing, clusters of 2
+    # options of the 512x512x1024 piston workload: KT + freq-weighted + super-absorbing, clusters of 2
     "kt_fw_sa_64x128": ((64, 128, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                              useSuperAbsorbing=True), 8e6, 10),
     "lie_water_96": ((96, 96, 192), dict(useSplitStep=False, alpha0=-1.0), 3e6, 8),
@@ -185,7 +185,7 @@ FAST_CASES = {
                                                          useSuperAbsorbing=True), 4e6, 6,
                                    dict(zs=[3.0e-4, 9.0e-4], amp=[False, True]),
                                    dict(zs=[5.0e-4, 1.2e-3])),
-    # configs[0]-like grid at full size (128^2 x 256) for a few steps
+    # the 128^2 x 256 piston workload's grid at full size for a few steps
     "c1_grid_tvd_wendland": ((128, 128, 256), dict(fluxScheme="rusanov", boundaryProfile="wendland",
                                                    dX=3.08e-4, dY=3.08e-4, f0=1e6), 4e5, 6),
 }
