@@ -94,15 +94,26 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
     const int npairs = M / 2 + 1;
     const size_t colA = (size_t)xq * Y + y0;        // row x
     const size_t colB = colA + (size_t)X2 * Y;       // row x + X/2
+    // two neighbouring columns per thread: 16-byte loads of (y, y+1)
 #pragma unroll 2
-    for (int it = tid; it < npairs * CY; it += nthr) {
-      const int u = it & (CY - 1), k = it / CY;
+    for (int it = tid; it < npairs * (CY / 2); it += nthr) {
+      const int u0 = 2 * (it & (CY / 2 - 1)), k = it / (CY / 2);
       const int k2 = M - k;
       const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
       const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
-      const float2* pk = p.spec + (size_t)sk * ncols + u;
-      const float2* pm = p.spec + (size_t)sk2 * ncols + u;
-      float2 xa = pk[colA], xb = pk[colB], ma = pm[colA], mb = pm[colB];
+      const float2* pk = p.spec + (size_t)sk * ncols + u0;
+      const float2* pm = p.spec + (size_t)sk2 * ncols + u0;
+      const float4 xa2 = *reinterpret_cast<const float4*>(pk + colA);
+      const float4 xb2 = *reinterpret_cast<const float4*>(pk + colB);
+      const float4 ma2 = *reinterpret_cast<const float4*>(pm + colA);
+      const float4 mb2 = *reinterpret_cast<const float4*>(pm + colB);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+      const int u = u0 + h;
+      float2 xa = h ? make_float2(xa2.z, xa2.w) : make_float2(xa2.x, xa2.y);
+      float2 xb = h ? make_float2(xb2.z, xb2.w) : make_float2(xb2.x, xb2.y);
+      float2 ma = h ? make_float2(ma2.z, ma2.w) : make_float2(ma2.x, ma2.y);
+      float2 mb = h ? make_float2(mb2.z, mb2.w) : make_float2(mb2.x, mb2.y);
       if (p.split_in) {
         const float2 tb = cmulc(xb, wx), tm = cmulc(mb, wx);
         const float2 a0 = xa, m0 = ma;
@@ -131,6 +142,7 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
           line[PL::pos(sk)] = make_float2((E.x - O.y) * (2.f * inv2M), (E.y + O.x) * (2.f * inv2M));
           line[PL::pos(sk2)] = make_float2((E.x + O.y) * (2.f * inv2M), (-E.y + O.x) * (2.f * inv2M));
         }
+      }
       }
     }
     __syncthreads();
@@ -201,13 +213,18 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
     const int npairs = M / 2 + 1;
     const size_t colA = (size_t)xq * Y + y0;
     const size_t colB = colA + (size_t)X2 * Y;
+    // two neighbouring columns per thread: 16-byte stores of (y, y+1)
 #pragma unroll 2
-    for (int it = tid; it < npairs * CY; it += nthr) {
-      const int u = it & (CY - 1), k = it / CY;
+    for (int it = tid; it < npairs * (CY / 2); it += nthr) {
+      const int u0 = 2 * (it & (CY / 2 - 1)), k = it / (CY / 2);
       const int k2 = M - k;
       const int sk = (k == 0) ? 0 : PL::slot_of_freq(k);
       const int sk2 = (k == 0) ? M : PL::slot_of_freq(k2);
       const float2 wk = (k == 0) ? make_float2(1.f, 0.f) : __ldg(twT + k);
+      float2 oa[2][2], ob[2][2];  // [h][bin k, bin M-k] of columns u0 + h
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+      const int u = u0 + h;
       float2 ra[2], rb[2];  // [0]: bin k, [1]: bin M-k, for rows x and x+X/2
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
@@ -241,13 +258,18 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
           rb[j] = b;
         }
       }
+      oa[h][0] = ra[0];
+      oa[h][1] = ra[1];
+      ob[h][0] = rb[0];
+      ob[h][1] = rb[1];
+      }
       float2* so = p.spec_out ? p.spec_out : p.spec;
-      float2* pk = so + (size_t)sk * ncols + u;
-      float2* pm = so + (size_t)sk2 * ncols + u;
-      pk[colA] = ra[0];
-      pk[colB] = rb[0];
-      pm[colA] = ra[1];
-      pm[colB] = rb[1];
+      float2* pk = so + (size_t)sk * ncols + u0;
+      float2* pm = so + (size_t)sk2 * ncols + u0;
+      *reinterpret_cast<float4*>(pk + colA) = make_float4(oa[0][0].x, oa[0][0].y, oa[1][0].x, oa[1][0].y);
+      *reinterpret_cast<float4*>(pk + colB) = make_float4(ob[0][0].x, ob[0][0].y, ob[1][0].x, ob[1][0].y);
+      *reinterpret_cast<float4*>(pm + colA) = make_float4(oa[0][1].x, oa[0][1].y, oa[1][1].x, oa[1][1].y);
+      *reinterpret_cast<float4*>(pm + colB) = make_float4(ob[0][1].x, ob[0][1].y, ob[1][1].x, ob[1][1].y);
     }
   }
 }
