@@ -197,7 +197,9 @@ typedef struct {
   int xy_clusters;   /* cap on resident CTA groups (clusters) of the L2-exchange plane kernel: 0..64 */
   int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..64 */
   int xy_sync;       /* group barrier of those kernels: 1 thread-block cluster, 2 counter
-                      * barrier in a cooperative launch (plans in a batch use 1) */
+                      * barrier in a cooperative launch, which is sized to fill the GPU
+                      * (plans in a batch use 1; so should a plan whose stream runs
+                      * beside other heavy work on the same GPU) */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of
