@@ -3,7 +3,7 @@ as-shipped FP32 precision of the reference and writes their metrics to
 known_answers.json, which the GPU tests compare against (the oracle itself is
 pinned bit for bit to the reference's FP32 run by the golden fixtures).
 
-    python tests/golden/make_known_answers.py            # all cases (~1 h on 8 cores)
+    python tests/golden/make_known_answers.py            # all cases (~25 min on 8 cores)
     python tests/golden/make_known_answers.py reflection convergence
 """
 import json
