@@ -942,6 +942,16 @@ static void set_flux(asg_plan* p, TParams& t, double dz, double beta_tvd, int fl
 static int nonlinear_stage(asg_plan* p, double dz, double beta_tvd, const float* axy,
                            const float* at) {
   const int flux = p->cfg.split_step ? p->cfg.flux : ASG_FLUX_RUSANOV;
+  if (p->N == 0.0) {
+    // linear medium (beta = 0): every flux adds -0 * dZ/dT * (flux difference)
+    // to the field, the identity for finite values (the KT step's halvings
+    // aside, which change only subnormal samples), so the pass only tapers
+    TParams t = tparams(p);
+    t.op.abl_xy = axy;
+    t.op.abl_t = at;
+    t.do_r2c = 1;
+    return run_t(p, t, ASG_K_T_NONLIN);
+  }
   if (!p->cfg.nonlinear_obliquity) {
     TParams t = tparams(p);
     t.op.abl_xy = axy;

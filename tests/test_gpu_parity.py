@@ -155,6 +155,10 @@ FAST_CASES = {
     "kt_fw_sa_64x128": ((64, 128, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                              useSuperAbsorbing=True), 8e6, 10),
     "lie_water_96": ((96, 96, 192), dict(useSplitStep=False, alpha0=-1.0), 3e6, 8),
+    # linear medium (beta = 0): the Burgers step is the identity and is skipped
+    "linear_kt_fw_sa_64x128": ((64, 128, 128), dict(beta=0.0, fluxScheme="kt",
+                                                    useFreqWeightedBoundary=True,
+                                                    useSuperAbsorbing=True), 2e6, 6),
     # planes too large for one CTA's shared memory: generic row and column passes
     # over HBM, the epilogue pass, screens and sources; and the power reduction
     "big_odd_kt_fw_sa": ((121, 119, 64), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
