@@ -17,6 +17,7 @@ ASG_OK = 0
 ERRORS = {
     -1: "ASG_ERR_ARG", -2: "ASG_ERR_SHAPE", -3: "ASG_ERR_NAN", -4: "ASG_ERR_STABILITY",
     -5: "ASG_ERR_TIMEOUT", -6: "ASG_ERR_CUDA", -7: "ASG_ERR_STATE", -8: "ASG_ERR_NOMEM",
+    -9: "ASG_ERR_SUBCYCLES",
 }
 FLUX_RUSANOV, FLUX_RUSANOV_TVD, FLUX_KT, FLUX_KT_MINMOD = 1, 2, 3, 4
 
@@ -30,6 +31,7 @@ EXPORTED = [
     "asg_net_param_count", "asg_net_create", "asg_net_destroy", "asg_net_set_params",
     "asg_net_get_params", "asg_net_forward", "asg_net_train_step", "asg_flux_columns_learned",
     "asg_net_set_output_scale", "asg_add_source_compact", "asg_debug_set_barrier_skew",
+    "asg_flux_columns_device_clamped",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -44,6 +46,12 @@ class StabilityError(ASGError):
     """N dZ/dT max|p| exceeded stabilityThreshold.  The reference restarts from
     z=0 with a step that cannot fall below dZmin, i.e. it never terminates
     (angular_spectrum_solver.py:1420-1439); this is reported instead."""
+
+
+class SubcycleCapError(ASGError):
+    """Per-column KT sub-cycling: some column needed more sub-cycles than the
+    cap and ran above its CFL target.  The run completed; the outputs exist
+    but do not meet the requested CFL target."""
 
 
 class Config(C.Structure):
@@ -116,6 +124,7 @@ def load(require_device: bool = True):
     lib.asg_flux_columns_device.argtypes = [P, P, C.c_int, C.c_int, C.c_int, C.c_double,
                                             C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, P]
+    lib.asg_flux_columns_device_clamped.argtypes = [P, C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
     lib.asg_get_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_debug_set_barrier_skew.argtypes = [P, C.c_int]
@@ -154,6 +163,8 @@ def check(code):
     msg = _lib.asg_last_error().decode(errors="replace") if _lib is not None else ""
     if code == -4:
         raise StabilityError(code, msg)
+    if code == -9:
+        raise SubcycleCapError(code, msg)
     raise ASGError(code, msg)
 
 

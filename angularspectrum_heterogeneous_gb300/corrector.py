@@ -140,6 +140,16 @@ def _flux_device(cols, out, n_coef, dz, dt, cfl_target, max_sub, flux=_lib.FLUX_
         C.c_void_p(cols.data_ptr()), C.c_void_p(out.data_ptr()), cols.shape[0], cols.shape[1],
         flux, float(n_coef), float(dz), float(dt), 1.0, float(cfl_target), int(max_sub),
         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    if cfl_target > 0.0:
+        # a target column capped at max_sub sub-cycles would not be the fully
+        # sub-cycled step the network is trained towards
+        n, need = C.c_uint(0), C.c_uint(0)
+        _lib.check(lib.asg_flux_columns_device_clamped(
+            C.c_void_p(torch.cuda.current_stream().cuda_stream), C.byref(n), C.byref(need)))
+        if n.value:
+            raise _lib.SubcycleCapError(
+                -9, f"{n.value} target columns needed up to {need.value} sub-cycles "
+                    f"(cap {max_sub})")
     return out
 
 

@@ -259,6 +259,7 @@ struct asg_plan {
   int* d_status_step = nullptr;
   double* d_iprev = nullptr;
   unsigned* d_hist = nullptr;
+  unsigned* d_clamp = nullptr;     // [2] columns capped at kt_max_subcycles, largest need
   // outputs
   float *o_pnp = nullptr, *o_ppp = nullptr, *o_pI = nullptr, *o_pIloss = nullptr, *o_pax = nullptr;
   int o_cap = 0;
@@ -346,7 +347,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
                   p->d_screens, p->d_src, p->d_step, p->d_max_cur, p->d_max_next,
-                  p->d_status, p->d_status_step, p->d_iprev, p->d_hist};
+                  p->d_status, p->d_status_step, p->d_iprev, p->d_hist, p->d_clamp};
   for (void* q : ptrs) cudaFree(q);
   free_outputs(p);
   cudaEventDestroy(p->ev0);
@@ -553,6 +554,8 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   CKS(dalloc(&p->d_status_step, 1));
   CKS(dalloc(&p->d_iprev, p->ncols));
   CKS(dalloc(&p->d_hist, 64));
+  CKS(dalloc(&p->d_clamp, 2));
+  CK(cudaMemsetAsync(p->d_clamp, 0, 2 * sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_status, 0, sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_hist, 0, 64 * sizeof(unsigned), p->st));
 
@@ -843,6 +846,7 @@ static TParams tparams(asg_plan* p) {
   t.op.max_subcycles = p->cfg.kt_max_subcycles > 0 ? p->cfg.kt_max_subcycles : 1024;
   t.op.cfl_target = (float)p->cfg.kt_cfl_target;
   t.op.subcycle_hist = p->d_hist;
+  t.op.subcycle_clamp = p->d_clamp;
   return t;
 }
 
@@ -1211,6 +1215,7 @@ static int prepare_run(asg_plan* p, const float* init, double prop_dist, double 
   CK(cudaMemsetAsync(p->d_max_cur, 0, sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_max_next, 0, sizeof(unsigned), p->st));
   CK(cudaMemsetAsync(p->d_status_step, 0, sizeof(int), p->st));
+  CK(cudaMemsetAsync(p->d_clamp, 0, 2 * sizeof(unsigned), p->st));
   CKS(copy_host(p->real, init, (size_t)p->ncols * p->T * sizeof(float), cudaMemcpyHostToDevice,
                 p->st));
   // initial upload: iprev, stability max, forward transform
@@ -1280,10 +1285,28 @@ static void step_done(asg_plan* p, RunState& rs, size_t k) {
   p->zaxis.push_back(rs.zcum);
 }
 
+// Columns whose per-column KT sub-cycle count was capped at kt_max_subcycles
+// ran above the CFL target: the run finished (outputs are complete) but is
+// reported, not passed off as meeting the target.
+static int clamp_to_error(const unsigned* d_clamp, int max_subcycles, cudaStream_t st) {
+  unsigned c[2] = {0u, 0u};
+  CK(cudaMemcpyAsync(c, d_clamp, sizeof(c), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (c[0] == 0u) return ASG_OK;
+  return fail(ASG_ERR_SUBCYCLES,
+              "%u column steps needed more KT sub-cycles than the cap of %d (up to %u) and ran "
+              "above the CFL target; raise the cap or the target",
+              c[0], max_subcycles, c[1]);
+}
+
 static int finish_run(asg_plan* p, const RunState& rs) {
   collect_kernel_times(p);
   p->nsteps = (int)rs.steps.size();
-  return status_to_error(p);
+  CKS(status_to_error(p));
+  if (p->cfg.kt_cfl_target > 0.0)
+    return clamp_to_error(p->d_clamp,
+                          p->cfg.kt_max_subcycles > 0 ? p->cfg.kt_max_subcycles : 1024, p->st);
+  return ASG_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1841,9 +1864,9 @@ extern "C" int asg_flux_columns(const float* in, float* out, int ncols, int nT, 
   const size_t n = (size_t)ncols * nT;
   CKS(dalloc(&d, n));
   CKS(dalloc(&dout, n));
-  CKS(dalloc(&st, 1));
+  CKS(dalloc(&st, 4));  // status word, then the sub-cycle cap counters [2]
   CKS(dalloc(&tw, nT));
-  CK(cudaMemset(st, 0, sizeof(unsigned)));
+  CK(cudaMemset(st, 0, 4 * sizeof(unsigned)));
   CK(cudaMemcpy(d, in, n * sizeof(float), cudaMemcpyHostToDevice));
   TParams t;
   memset(&t, 0, sizeof(t));
@@ -1864,18 +1887,22 @@ extern "C" int asg_flux_columns(const float* in, float* out, int ncols, int nT, 
   t.op.n_kt64 = n_coef / dt;
   t.op.cfl_target = (float)cfl_target;
   t.op.max_subcycles = max_subcycles > 0 ? max_subcycles : 1024;
+  t.op.subcycle_clamp = st + 1;
   GenPlan gp = make_gen_plan(nT);
   int s = asg_launch_t(t, false, gp, 0);
   cudaError_t e = cudaDeviceSynchronize();
   if (s == ASG_OK && e == cudaSuccess)
     e = cudaMemcpy(out, dout, n * sizeof(float), cudaMemcpyDeviceToHost);
+  int sc = ASG_OK;
+  if (s == ASG_OK && e == cudaSuccess && cfl_target > 0.0)
+    sc = clamp_to_error(st + 1, t.op.max_subcycles, 0);
   cudaFree(d);
   cudaFree(dout);
   cudaFree(st);
   cudaFree(tw);
   if (s != ASG_OK) return fail(s, "flux kernel launch failed");
   if (e != cudaSuccess) return fail(ASG_ERR_CUDA, "%s", cudaGetErrorString(e));
-  return ASG_OK;
+  return sc;
 }
 
 // ---------------------------------------------------------------------------
@@ -1887,41 +1914,32 @@ extern "C" int asg_flux_columns(const float* in, float* out, int ncols, int nT, 
 // to its own pool, a real-time loop in which cudaMalloc/cudaFree (which
 // synchronise the device) are not allowed, or code that queues work on a
 // stream it must not stall. They call this entry point instead. Besides its
-// input and output the column kernel touches two small global areas: a status
-// word it reads first (it must be zero, or the kernel returns without work)
-// and a twiddle area it copies into shared memory (unused here, since the
-// columns go in and out as real samples with no transform). Both live in the
-// fixed array below, whose device address is looked up once per device.
+// input and output the column kernel touches three small global areas: a
+// status word it reads first (it must be zero, or the kernel returns without
+// work), the sub-cycle cap counters it adds to, and a twiddle area it copies
+// into shared memory (unused here, since the columns go in and out as real
+// samples with no transform). All live in the fixed array below.
 // ---------------------------------------------------------------------------
 static constexpr int FLUX_SCRATCH_MAX_NT = 2048;  // longest column of the kernel
-static constexpr int FLUX_SCRATCH_MAX_DEVICES = 64;
 
 struct FluxScratch {
   unsigned status;        // must read zero when the kernel starts
-  unsigned pad[63];       // keeps the twiddle area on its own 256-byte line
+  unsigned clamp[2];      // columns capped at max_subcycles, largest count needed
+  unsigned pad[61];       // keeps the twiddle area on its own 256-byte line
   float2 tw[FLUX_SCRATCH_MAX_NT];
 };  // 16,640 bytes in all
 
 static __device__ __align__(256) FluxScratch g_flux_scratch;
 
-static std::mutex g_flux_scratch_mu;
-static FluxScratch* g_flux_scratch_ptr[FLUX_SCRATCH_MAX_DEVICES];
-
-// Address of the scratch on the current device, looked up on the first call
-// made with that device current.
+// Device address of the scratch in the current context.  Looked up on every
+// call (cudaGetSymbolAddress allocates nothing): an address kept from an
+// earlier call would be stale after cudaDeviceReset or under another context.
+// The first call on a device also loads the library's kernels there, so make
+// it before any stream capture.
 static int flux_scratch_on_current_device(FluxScratch** out) {
-  int dev = -1;
-  CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= FLUX_SCRATCH_MAX_DEVICES)
-    return fail(ASG_ERR_ARG, "device ordinal %d is beyond the %d devices supported", dev,
-                FLUX_SCRATCH_MAX_DEVICES);
-  std::lock_guard<std::mutex> lock(g_flux_scratch_mu);
-  if (!g_flux_scratch_ptr[dev]) {
-    void* ptr = nullptr;
-    CK(cudaGetSymbolAddress(&ptr, g_flux_scratch));
-    g_flux_scratch_ptr[dev] = static_cast<FluxScratch*>(ptr);
-  }
-  *out = g_flux_scratch_ptr[dev];
+  void* ptr = nullptr;
+  CK(cudaGetSymbolAddress(&ptr, g_flux_scratch));
+  *out = static_cast<FluxScratch*>(ptr);
   return ASG_OK;
 }
 
@@ -1936,10 +1954,25 @@ extern "C" int asg_flux_columns_device(const float* d_in, float* d_out, int ncol
                 FLUX_SCRATCH_MAX_NT);
   if (flux < ASG_FLUX_RUSANOV || flux > ASG_FLUX_KT_MINMOD)
     return fail(ASG_ERR_ARG, "unknown flux %d", flux);
+  {
+    // with overlapping ranges a block's output columns could overwrite input
+    // columns that another block has not read yet
+    const size_t bytes = (size_t)ncols * (size_t)nT * sizeof(float);
+    const uintptr_t a = reinterpret_cast<uintptr_t>(d_in), b = reinterpret_cast<uintptr_t>(d_out);
+    if (a < b + bytes && b < a + bytes)
+      return fail(ASG_ERR_ARG, "d_in and d_out overlap (the step is not in place)");
+  }
+  {
+    // an error left pending by earlier work is not this call's failure
+    const cudaError_t pre = cudaPeekAtLastError();
+    if (pre != cudaSuccess)
+      return fail(ASG_ERR_CUDA, "a CUDA error was pending before this call: %s",
+                  cudaGetErrorString(pre));
+  }
   FluxScratch* scr = nullptr;
   CKS(flux_scratch_on_current_device(&scr));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  CK(cudaMemsetAsync(&scr->status, 0, sizeof(unsigned), st));
+  CK(cudaMemsetAsync(scr, 0, 3 * sizeof(unsigned), st));  // status and cap counters
   TParams t;
   memset(&t, 0, sizeof(t));
   t.ncols = ncols;
@@ -1959,12 +1992,28 @@ extern "C" int asg_flux_columns_device(const float* d_in, float* d_out, int ncol
   t.op.n_kt64 = n_coef / dt;
   t.op.cfl_target = (float)cfl_target;
   t.op.max_subcycles = max_subcycles > 0 ? max_subcycles : 1024;
+  t.op.subcycle_clamp = scr->clamp;
   GenPlan gp = make_gen_plan(nT);
   const int s = asg_launch_t(t, false, gp, st);
   if (s != ASG_OK) {
-    const cudaError_t e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();  // this call's own launch error
     return fail(s, "flux kernel launch failed: %s", cudaGetErrorString(e));
   }
+  return ASG_OK;
+}
+
+extern "C" int asg_flux_columns_device_clamped(void* stream, unsigned* n_clamped,
+                                               unsigned* max_needed) {
+  g_err.clear();
+  if (!n_clamped) return fail(ASG_ERR_ARG, "null argument");
+  FluxScratch* scr = nullptr;
+  CKS(flux_scratch_on_current_device(&scr));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned c[2] = {0u, 0u};
+  CK(cudaMemcpyAsync(c, scr->clamp, sizeof(c), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *n_clamped = c[0];
+  if (max_needed) *max_needed = c[1];
   return ASG_OK;
 }
 

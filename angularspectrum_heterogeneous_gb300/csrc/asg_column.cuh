@@ -56,6 +56,8 @@ struct ColumnOps {
   double* iprev;                    // [ncols]
   unsigned* max_next;               // stability max of the field entering the next step
   unsigned* subcycle_hist;          // optional [64] histogram of per-column sub-cycles
+  unsigned* subcycle_clamp;         // optional [2]: columns whose sub-cycle count was capped at
+                                    // max_subcycles, and the largest count one of them needed
   int init_stats;                   // first upload: only iprev / max_next
 };
 
@@ -418,6 +420,11 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
         if (!(cfl <= op.cfl_target || um < 1e-30f)) {
           float q = ceilf(cfl / op.cfl_target);
           nsub = (q > (float)op.max_subcycles) ? op.max_subcycles : (int)q;
+          // a capped column runs above its CFL target: counted for the host
+          if (q > (float)op.max_subcycles && op.subcycle_clamp != nullptr && lane == 0) {
+            atomicAdd(op.subcycle_clamp, 1u);
+            atomicMax(op.subcycle_clamp + 1, q < 4.0e9f ? (unsigned)q : 0xffffffffu);
+          }
         }
         if (op.subcycle_hist != nullptr && lane == 0)
           atomicAdd(op.subcycle_hist + min(nsub, 63), 1u);

@@ -90,11 +90,15 @@ def initial_step(initial_field, params) -> float:
 # process: later plans with the same key start from them.
 TUNING_CACHE = {}
 
+# Host wall-clock seconds of the phases of the last angular_spectrum_solve
+# call (plan and operators, march with the field upload, output read-back).
+LAST_SOLVE_TIMINGS = {}
+
 
 class Plan:
     """One GPU plan: grid, options, operators, screens and sources."""
 
-    def __init__(self, shape, params, kt_cfl_target: float = 0.0, kt_max_subcycles: int = 64):
+    def __init__(self, shape, params, kt_cfl_target: float = 0.0, kt_max_subcycles: int = 1024):
         self.lib = _lib.load()
         nX, nY, nT = shape
         self.shape = (nX, nY, nT)
@@ -270,7 +274,7 @@ def _torch_view(ptr, shape):
     return torch.as_tensor(_Dev(), device="cuda")
 
 
-def _prepared_plan(u0, params, kt_cfl_target=0.0, kt_max_subcycles=64):
+def _prepared_plan(u0, params, kt_cfl_target=0.0, kt_max_subcycles=1024):
     """A plan with the step operators (regular and partial step), screens and
     sources of one solve; returns (plan, dZ, step sequence)."""
     dz = initial_step(u0, params)
@@ -342,7 +346,7 @@ class Batch:
 
 
 def solve_batch(initial_fields, params_list, kt_cfl_target: float = 0.0,
-                kt_max_subcycles: int = 64, return_timing: bool = False):
+                kt_max_subcycles: int = 1024, return_timing: bool = False):
     """`angular_spectrum_solve` of many independent instances (uneven grids
     allowed) in one batched march.  Returns one output tuple per instance,
     each exactly as `angular_spectrum_solve` returns it (and the device time
@@ -397,6 +401,7 @@ def angular_spectrum_solve(
     if u0.ndim != 3:
         raise ValueError("initial_field must be (nX, nY, nT)")
     nX, nY, nT = u0.shape
+    t_start = _time.perf_counter()
     plan, dz, steps = _prepared_plan(u0, params)
     try:
         cb = None
@@ -404,8 +409,15 @@ def angular_spectrum_solve(
             def cb(user, step, z, ptr):
                 per_step_callback(step, z, _torch_view(ptr, (nX, nY, nT)))
         t0 = _time.time()
+        t_plan = _time.perf_counter()
         plan.run(u0, params.propDist, dz, cb)
+        t_run = _time.perf_counter()
         out = plan.outputs()
+        t_out = _time.perf_counter()
+        LAST_SOLVE_TIMINGS.clear()
+        LAST_SOLVE_TIMINGS.update(plan_s=t_plan - t_start, run_s=t_run - t_plan,
+                                  march_device_s=plan.last_run_ms() / 1e3,
+                                  outputs_s=t_out - t_run)
         if verbose:
             z = 0.0
             for cc, d in enumerate(steps):

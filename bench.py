@@ -145,7 +145,8 @@ def peaks():
 CPU_SAMPLE_GRID = (128, 128, 1024)
 
 
-def cpu_march(nsteps=1, threads=None, grid=CPU_SAMPLE_GRID, max_seconds=None):
+def cpu_march(nsteps=1, threads=None, grid=CPU_SAMPLE_GRID, max_seconds=None,
+              backend="scipy"):
     """March steps of the workload's options and time axis on a central
     sub-grid of the workload (the per-voxel cost of the FFT-based march is
     nearly size independent), by the oracle port of the reference (numpy +
@@ -154,7 +155,8 @@ def cpu_march(nsteps=1, threads=None, grid=CPU_SAMPLE_GRID, max_seconds=None):
     voxel-steps/s list, cores, sample description)."""
     import oracle.asm_oracle as O
     threads = threads or os.cpu_count()
-    O.set_fft_backend("scipy", threads)
+    if backend == "scipy":
+        O.set_fft_backend("scipy", threads)
     rates = []
     try:
         p = workload_params()
@@ -177,8 +179,9 @@ def cpu_march(nsteps=1, threads=None, grid=CPU_SAMPLE_GRID, max_seconds=None):
     vox = gx * gy * gt
     return rates, threads, (
         f"march steps of the workload's options on its central {gx}x{gy}x{gt} sub-grid "
-        f"({vox / 1e6:.1f} M voxels), oracle port of the reference (numpy, scipy.fft "
-        f"workers={threads}), operator build ({tb:.1f} s) and one warm-up step excluded; "
+        f"({vox / 1e6:.1f} M voxels), oracle port of the reference (numpy, "
+        + (f"scipy.fft workers={threads}" if backend == "scipy" else "numpy FFT, 1 thread")
+        + f"), operator build ({tb:.1f} s) and one warm-up step excluded; "
         f"median of {len(rates)} step(s)")
 
 
@@ -194,15 +197,64 @@ def run_reference_arm(args):
     # each timed step: one march step of the CPU sample, capped at ~2 minutes
     rates, cores, sample = cpu_march(args.steps, max_seconds=120)
     v = float(np.median(rates))
+    gx, gy, gt = CPU_SAMPLE_GRID
+    # the same sample single-threaded (numpy's pocketfft, one core), one step
+    r1, _, _ = cpu_march(1, threads=1, backend="numpy")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "voxel-steps/s",
             "n_gpus": args.gpus, "steps": len(rates), "warmup": 1,
-            "ms_per_step": V / v * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(),
+            "ms_per_step": gx * gy * gt / v * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config({"timed_grid": list(CPU_SAMPLE_GRID)}),
+            "ms_per_step_note": f"one march step of the timed {gx}x{gy}x{gt} sub-grid",
+            "ms_per_step_full_grid_extrapolated": V / v * 1e3,
             "cpu_baseline": {"value": v, "unit": "voxel-steps/s", "cores": cores,
                              "kind": "port", "sample": sample},
+            "cpu_single_thread": {"value": float(np.median(r1)), "unit": "voxel-steps/s",
+                                  "cores": 1, "kind": "port",
+                                  "sample": "one step of the same sub-grid, numpy FFT, 1 thread"},
             "e2e": {"value": v, "unit": "voxel-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# cuFFT comparison: one spectral stage through torch.fft (cuFFT)
+# ---------------------------------------------------------------------------
+def cufft_stage_ms(u0, reps=5):
+    """One spectral stage of the march written with torch.fft (cuFFT): rfft
+    along t, fft2 over (x, y), a complex multiplier, ifft2, irfft along t, on
+    the workload's field resident in HBM; the median of `reps` CUDA-event
+    timings after two warm-up stages.  Only a comparison: the march itself
+    never calls cuFFT."""
+    import torch
+    u = torch.from_numpy(u0).cuda()
+    nt = u.shape[2]
+    g = torch.Generator(device="cuda").manual_seed(0)
+    ph = torch.rand((u.shape[0], u.shape[1], nt // 2 + 1), device="cuda", generator=g)
+    table = torch.polar(torch.ones_like(ph), ph * 6.283185307179586)
+    del ph
+
+    def stage(x):
+        s = torch.fft.rfft(x, dim=2)
+        s = torch.fft.fft2(s, dim=(0, 1))
+        s *= table
+        s = torch.fft.ifft2(s, dim=(0, 1))
+        return torch.fft.irfft(s, n=nt, dim=2)
+
+    for _ in range(2):
+        u = stage(u)
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        u = stage(u)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    del u, table
+    torch.cuda.empty_cache()
+    return float(np.median(times))
 
 
 # ---------------------------------------------------------------------------
@@ -253,6 +305,7 @@ def run_gpu_arm(args):
 
     # e2e: public API, host buffers in and out, K steps
     e2e_s, h2d, d2h = float("nan"), 0, 0
+    e2e_phases = None
     if not args.no_e2e:
         p2 = workload_params()
         p2.propDist = args.steps * dz
@@ -263,6 +316,17 @@ def run_gpu_arm(args):
         e2e_s = time.time() - t0
         h2d = u0.nbytes / args.steps
         d2h = sum(a.nbytes for a in out) / args.steps
+        from angularspectrum_heterogeneous_gb300.solver import LAST_SOLVE_TIMINGS
+        e2e_phases = dict(LAST_SOLVE_TIMINGS)
+        del out
+    cufft = None
+    if not args.no_cufft and world == 1:
+        ours = sum(stats[k][0] / stats[k][1] for k in ("xy_A", "t_mid") if stats[k][1])
+        cufft = {"ms": cufft_stage_ms(u0), "ours_ms": ours,
+                 "what": "one spectral stage (rfft t, fft2 xy, multiplier, ifft2, irfft t) "
+                         "through torch.fft/cuFFT on the same 512x512x1024 field, against "
+                         "this library's plane pass xy_A + column pass t_mid (which also "
+                         "applies the taper); not part of the headline"}
 
     peak, peak_kind = peaks()
     kinds = {k: v for k, v in stats.items() if v[1] > 0 and k != "other"}
@@ -290,7 +354,9 @@ def run_gpu_arm(args):
                          "step_frac": value * B_ALG / 1e9 / peak},
             "kernels": per_kernel,
             "e2e": {"value": V * args.steps / e2e_s, "unit": "voxel-steps/s",
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "phases_s": e2e_phases if not args.no_e2e else None},
+            "cufft_comparison": cufft,
             "gpu_launches": int(launches),
             "clocks": clk.summary()}
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -564,6 +630,19 @@ def run_hetero_arm(args):
     print(json.dumps(line))
 
 
+def rank_launch_command(argv, n, port=None):
+    """The torchrun command that runs this script as n ranks on one node (one
+    per GPU, LOCAL_RANK = GPU index), rendezvous on 127.0.0.1."""
+    if port is None:
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+            f"--nproc-per-node={n}", "--master-addr=127.0.0.1", f"--master-port={port}",
+            os.path.abspath(__file__), *argv]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -575,12 +654,22 @@ def main():
                     help="profiling only: a smaller grid with the same options")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-cufft", action="store_true")
+    ap.add_argument("--print-rank-env", action="store_true",
+                    help="each rank prints its RANK/LOCAL_RANK/WORLD_SIZE and exits")
     ap.add_argument("--workload", default="plain",
                     choices=["plain", "batch", "learned", "hetero"],
                     help="batch: the 64-instance batched march; learned: the learned KT "
                          "step against the plain one; hetero: the transcranial bowl with "
                          "skull screens (none is the headline line)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torchrun
+        sys.exit(subprocess.call(rank_launch_command(sys.argv[1:], args.gpus)))
+    if args.print_rank_env:
+        print(json.dumps({k: os.environ.get(k) for k in
+                          ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR")}), flush=True)
+        return
     if args.grid:
         set_grid(*args.grid)
     if args.workload == "batch" and args.impl != "reference":

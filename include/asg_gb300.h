@@ -48,7 +48,10 @@ typedef enum {
   ASG_ERR_TIMEOUT = -5,    /* a bounded device wait gave up */
   ASG_ERR_CUDA = -6,       /* CUDA runtime error */
   ASG_ERR_STATE = -7,      /* call out of order (e.g. run before operators) */
-  ASG_ERR_NOMEM = -8       /* device allocation failed */
+  ASG_ERR_NOMEM = -8,      /* device allocation failed */
+  ASG_ERR_SUBCYCLES = -9   /* per-column KT sub-cycling: a column needed more sub-cycles
+                            * than the cap and ran above the CFL target (the outputs are
+                            * complete; the run is reported, not silently accepted) */
 } asg_status;
 
 typedef struct asg_plan asg_plan;
@@ -75,7 +78,8 @@ typedef struct {
   double stability_threshold;
   double adaptive_filter_strength; /* enters the per-step TVD parameter beta_tvd */
   double kt_cfl_target;      /* > 0: per-column KT sub-cycling at this CFL (extension) */
-  int kt_max_subcycles;
+  int kt_max_subcycles;      /* cap on a column's sub-cycle count (0: 1024); a column that
+                              * needs more makes asg_run return ASG_ERR_SUBCYCLES */
   int pax_x, pax_y;          /* column recorded in pax (reference: nX//2, nY//2) */
 } asg_config;
 
@@ -228,25 +232,38 @@ int asg_autotune(asg_plan* plan, const float* field, double dz, int steps, asg_t
 int asg_apply_operator(asg_plan* plan, int op, float* field, int screen_index,
                        double* scalar_out);
 
-/* Burgers step on ncols independent columns of length nT (host in/out). */
+/* Burgers step on ncols independent columns of length nT (host in/out).  With
+ * cfl_target > 0 each column is sub-cycled at that CFL; a column that needs more
+ * than max_subcycles makes the call return ASG_ERR_SUBCYCLES (out is written). */
 int asg_flux_columns(const float* in, float* out, int ncols, int nT, int flux, double n_coef,
                      double dz, double dt, double beta_tvd, double cfl_target, int max_subcycles);
 
 /* The same Burgers step on DEVICE buffers (ncols x nT floats each, column-major
- * as above; d_in == d_out is not allowed), queued on `stream` (a cudaStream_t;
- * NULL = the legacy default stream). No counterpart in the reference: it exists
- * for callers that must not allocate device memory (memory owned by their own
- * pool, loops where a synchronising cudaMalloc/cudaFree is not allowed).
- * It allocates nothing: its scratch (a status word it clears on `stream` before
- * each launch, and a twiddle area) is a fixed 16,640-byte array in the library,
- * whose address is looked up on the first call made with each device current,
- * so make that first call before any stream capture. nT above 2048 is rejected
- * with ASG_ERR_SHAPE. Returns once the work is queued; the result is ready when
- * `stream` is. Two calls in flight at once on one device (different streams or
- * host threads) share the scratch and race: order them on one stream. */
+ * as above; overlapping d_in and d_out ranges are rejected with ASG_ERR_ARG),
+ * queued on `stream` (a cudaStream_t; NULL = the legacy default stream). No
+ * counterpart in the reference: it exists for callers that must not allocate
+ * device memory (memory owned by their own pool, loops where a synchronising
+ * cudaMalloc/cudaFree is not allowed).
+ * It allocates nothing: its scratch (a status word and the sub-cycle cap
+ * counters, which it clears on `stream` before each launch, and a twiddle area)
+ * is a fixed 16,640-byte array in the library. Its device address is looked up
+ * on every call; the first call on a device also loads the library's kernels
+ * there, so make that first call before any stream capture. nT above 2048 is
+ * rejected with ASG_ERR_SHAPE; an error left pending by earlier CUDA work is
+ * reported (ASG_ERR_CUDA) without launching and without clearing it. Returns
+ * once the work is queued; the result is ready when `stream` is. Two calls in
+ * flight at once on one device (different streams or host threads) share the
+ * scratch and race: order them on one stream. */
 int asg_flux_columns_device(const float* d_in, float* d_out, int ncols, int nT, int flux,
                             double n_coef, double dz, double dt, double beta_tvd,
                             double cfl_target, int max_subcycles, void* stream);
+
+/* Sub-cycle cap counters of the last asg_flux_columns_device call on the current
+ * device, read after `stream` (the stream that call used) completes: the number
+ * of columns whose sub-cycle count was capped at max_subcycles (they ran above
+ * cfl_target) and, if max_needed is not NULL, the largest count one of them
+ * needed.  No counterpart in the reference. */
+int asg_flux_columns_device_clamped(void* stream, unsigned* n_clamped, unsigned* max_needed);
 
 /* ---- learned KT corrector (no counterpart in the reference) ------------------
  * A 1-D convolutional network along t (1 -> 64 -> 64 -> 64 -> 1 channels,

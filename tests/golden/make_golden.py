@@ -5,8 +5,9 @@ as shipped in a machine without JAX: it imports ``jax`` and a missing
 ``tof_extraction`` module.  This script installs a small numpy-backed stand-in
 for the handful of ``jax``/``jax.numpy`` names the module uses
 (``jit`` -> identity, ``jnp.*`` -> numpy, functional ``.at[idx].set/add``
-updates) and a stub ``tof_extraction``, imports the reference from
-``REFERENCE_DIR`` (default ``/root/reference``), runs a fixed set of seeded
+updates) and a stub ``tof_extraction``, imports the reference from the
+directory given by ``--reference-dir`` or the ``ASG_REFERENCE_DIR``
+environment variable (one of them is required), runs a fixed set of seeded
 small scenarios and writes the inputs and outputs to ``*.npz`` files next to
 this script.
 
@@ -15,7 +16,8 @@ committed; the GPU machine never needs the reference.  Two precisions are
 produced: ``fp32`` runs the module as shipped; ``fp64`` remaps the module's
 float32/complex64 casts to float64/complex128 (the FP64 oracle).
 
-Run:  python tests/golden/make_golden.py  [--reference-dir DIR]
+Run:  python tests/golden/make_golden.py  --reference-dir DIR
+      (or ASG_REFERENCE_DIR=DIR python tests/golden/make_golden.py)
 """
 from __future__ import annotations
 
@@ -287,10 +289,12 @@ def gen_builders(ref, out):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference-dir", default=os.environ.get("ASG_REFERENCE_DIR",
-                                                              "/root/reference"))
+    ap.add_argument("--reference-dir", default=os.environ.get("ASG_REFERENCE_DIR"),
+                    help="directory holding angular_spectrum_solver.py (or ASG_REFERENCE_DIR)")
     ap.add_argument("--only", default=None, help="comma list of solve scenarios")
     args = ap.parse_args()
+    if not args.reference_dir:
+        ap.error("give --reference-dir or set ASG_REFERENCE_DIR")
     which = args.only.split(",") if args.only else None
     for fp64 in (False, True):
         ref = load_reference(args.reference_dir, fp64)

@@ -44,6 +44,37 @@ def test_flux_columns_vs_reference(lib, nT):
             assert rel(out, ref) < 2e-6, (key, t, rel(out, ref))
 
 
+def test_flux_subcycle_cap_is_reported(lib):
+    """A column that needs more sub-cycles than the cap is reported
+    (ASG_ERR_SUBCYCLES), not run silently above its CFL target."""
+    from angularspectrum_heterogeneous_gb300 import SubcycleCapError, _lib
+    N = 3.5 / (2 * 1540.0 ** 3 * 1000.0)
+    cols = np.stack([S.seeded_column(256, s) * 6.0 for s in range(4)]).astype(np.float32)
+    with pytest.raises(SubcycleCapError):
+        _lib.flux_columns(cols, _lib.FLUX_KT, N, 4e-4, 1e-8, cfl_target=1e-3, max_subcycles=2)
+    _lib.flux_columns(cols, _lib.FLUX_KT, N, 4e-4, 1e-8, cfl_target=1e-3, max_subcycles=4096)
+
+
+def test_march_subcycle_cap_is_reported(lib):
+    from angularspectrum_heterogeneous_gb300 import Plan, SubcycleCapError
+    nX, nY, nT = 32, 64, 128
+    kw = dict(S.BASE)
+    kw.update(fluxScheme="kt", propDist=3 * kw["dZmin"])
+    u0 = S.piston_field(nX, nY, nT, kw["dX"], kw["dY"], kw["dT"], kw["f0"], 8e6,
+                        radius=0.35 * nX * kw["dX"], focus=8e-3)
+    for cap, raises in [(1, True), (4096, False)]:
+        plan = Plan((nX, nY, nT), solver_params(kw), kt_cfl_target=1e-3, kt_max_subcycles=cap)
+        try:
+            plan.set_operators(0, kw["dZmin"])
+            if raises:
+                with pytest.raises(SubcycleCapError):
+                    plan.run(u0, kw["propDist"], kw["dZmin"])
+            else:
+                plan.run(u0, kw["propDist"], kw["dZmin"])
+        finally:
+            plan.close()
+
+
 def test_flux_per_column_subcycles(lib):
     """Per-column CFL sub-cycling: each column its own sub-step count."""
     from angularspectrum_heterogeneous_gb300 import _lib
@@ -147,6 +178,9 @@ def test_solve_vs_reference_fixtures(lib, name):
 # ---------------------------------------------------------------------------
 # full solves on the fast kernels against the oracle run live (FP64)
 # ---------------------------------------------------------------------------
+C2_OPTS = dict(fluxScheme="kt", useFreqWeightedBoundary=True, useSuperAbsorbing=True,
+               dX=1.5e-4, dY=1.5e-4, dT=1e-8, f0=2e6, dZmin=1e-4)
+
 FAST_CASES = {
     # options of the 128x128x256 piston workload on a 64^2 x 128 grid
     "tvd_wendland_64": ((64, 64, 128), dict(fluxScheme="rusanov", boundaryProfile="wendland"),
@@ -192,6 +226,14 @@ FAST_CASES = {
     # the 128^2 x 256 piston workload's grid at full size for a few steps
     "c1_grid_tvd_wendland": ((128, 128, 256), dict(fluxScheme="rusanov", boundaryProfile="wendland",
                                                    dX=3.08e-4, dY=3.08e-4, f0=1e6), 4e5, 6),
+    # the kernel instantiations of the 512x512x1024 KT workload (KT, freq-weighted,
+    # super-absorbing, Strang; its dX, dT and f0):
+    # 1024-sample columns (the column passes' 512-point complex plan, 16 columns per block)
+    "c2_columns_32x128x1024": ((32, 128, 1024), C2_OPTS, 2e6, 8),
+    # 512-wide planes: cooperative groups of 16 CTAs over 256-row half-planes
+    "c2_planes_512x512x128": ((512, 512, 128), C2_OPTS, 2e6, 2),
+    # 384-wide planes: cooperative groups of 12 CTAs
+    "c2_planes_384x384x64": ((384, 384, 64), C2_OPTS, 2e6, 3),
 }
 
 

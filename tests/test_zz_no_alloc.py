@@ -68,3 +68,38 @@ def test_device_entry_rejects_long_columns():
     code = _device_call(lib, d, d, 2, 4096, _lib.FLUX_KT, 1e-4, 1e-8)
     assert code == -2  # ASG_ERR_SHAPE
     assert b"2048" in lib.asg_last_error()
+
+
+def test_device_entry_rejects_overlapping_buffers():
+    import torch
+    from angularspectrum_heterogeneous_gb300 import _lib
+    lib = _lib.load()
+    nT, ncols = 256, 8
+    d = torch.zeros(ncols * nT + nT, device="cuda")
+    assert _device_call(lib, d, d, ncols, nT, _lib.FLUX_KT, 1e-4, 1e-8) == -1  # same buffer
+    assert _device_call(lib, d, d[nT:], ncols, nT, _lib.FLUX_KT, 1e-4, 1e-8) == -1  # shifted
+    assert b"overlap" in lib.asg_last_error()
+
+
+def test_device_entry_reports_capped_subcycles():
+    """Columns that need more sub-cycles than the cap are counted in the fixed
+    scratch; the count is read after the stream completes, and the next call
+    starts again from zero."""
+    import torch
+    from angularspectrum_heterogeneous_gb300 import _lib
+    lib = _lib.load()
+    nT, ncols = 256, 16
+    cols = _columns(ncols, nT)
+    stream = torch.cuda.current_stream()
+    d_in = torch.from_numpy(cols).cuda()
+    d_out = torch.empty_like(d_in)
+    n, need = C.c_uint(0), C.c_uint(0)
+    for cap, expect_capped in [(2, True), (4096, False)]:
+        _lib.check(_device_call(lib, d_in, d_out, ncols, nT, _lib.FLUX_KT, 4e-4, 1e-8,
+                                cfl_target=1e-3, max_subcycles=cap, stream=stream.cuda_stream))
+        _lib.check(lib.asg_flux_columns_device_clamped(C.c_void_p(stream.cuda_stream),
+                                                       C.byref(n), C.byref(need)))
+        if expect_capped:
+            assert n.value > 0 and need.value > cap, (n.value, need.value)
+        else:
+            assert n.value == 0, n.value
