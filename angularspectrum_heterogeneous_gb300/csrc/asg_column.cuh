@@ -123,19 +123,23 @@ ASG_DEV float kt_slope(float um1, float u0, float up1) {
                      : fminf(fabsf(dm), fabsf(dp));
   return (dm * dp > 0.f) ? copysignf(m, dm) : 0.f;
 }
-// KT interface flux from the reconstructed states (:772-793)
+// KT interface flux from the reconstructed states (:772-793), for Burgers'
+// flux f(u) = -u^2/2, whose speeds are a = -u.  With aL = -um, aR = -up the
+// reference forms ap = max(aL, aR, 0), am = min(aL, aR, 0) and divides
+// (ap fm - am fp - ap am (up - um)) / (ap - am); for this flux the quotient is
+// a polynomial in each sign case (exact algebra, no division):
+//   um, up <= 0 (both speeds >= 0):            fm = -um^2/2
+//   um, up >= 0 (both speeds <= 0):            fp = -up^2/2
+//   um < 0 < up (aL > 0 > aR):  (-um^3/2 + ... )/(aL - aR) = -(um^2 + 3 um up + up^2)/2
+//   um > 0 > up (aL < 0 < aR):                            =  3/2 um up
+// The reference's Lax-Friedrichs branch (ap - am < 1e-14) differs from these
+// only where |um| and |up| are below 1e-14, where both fluxes are below 1e-28.
 ASG_DEV float kt_fh(float um, float up) {
-  float ap = fmaxf(fmaxf(-um, -up), 0.f);
-  float am = fminf(fminf(-um, -up), 0.f);
-  float fm = -0.5f * um * um;
-  float fp = -0.5f * up * up;
-  float den = ap - am;
-  bool small = fabsf(den) < 1e-14f;
-  if (small) {
-    return 0.5f * (fm + fp) - 0.5f * fmaxf(fabsf(um), fabsf(up)) * (up - um);
-  }
-  // den >= 1e-14 here: the approximate quotient (2 ulp) is safe
-  return __fdividef(ap * fm - am * fp - ap * am * (up - um), den);
+  const float q = um * up;
+  const float m2 = um * um, p2 = up * up;
+  const float same = -0.5f * ((um + up <= 0.f) ? m2 : p2);
+  const float mixed = (um < 0.f) ? fmaf(-0.5f, m2 + p2, -1.5f * q) : 1.5f * q;
+  return (q >= 0.f) ? same : mixed;
 }
 
 // ---------------------------------------------------------------------------
@@ -355,6 +359,74 @@ ASG_DEV void kt_column_step_chunk(const Col& col, int nT, float ndt, float dz, u
   __syncwarp(mask);
 }
 
+// One SSP-RK2 KT step of size dz in a single streaming pass, in place, for a
+// column of exactly nT = 32 CH samples (CH >= 4); lane l owns samples
+// [l CH, (l+1) CH).  Stage 2 at t needs stage-1 values s1 at t-2..t+2, which
+// need u at t-4..t+4, so each lane walks its run once with sliding windows:
+// iteration t loads u[t+4], forms the slope at t+3, the flux at t+5/2 and
+// s1[t+2], then the slope of s1 at t+1, its flux at t+1/2 and the new u[t].
+// About 25 values stay live instead of the whole run.  The four samples on
+// either side of a run come from the neighbouring lanes by shuffles before
+// any write (every later read is of the lane's own, not yet written,
+// samples); the lane recomputes s1 at t0-2, t0-1 (a short prologue).  The
+// column ends t = 0 and nT-1 keep zero slope and zero rhs, as in the reference
+// (:758-839).
+template <int CH, bool MC, class Col>
+ASG_DEV void kt_step_stream(const Col& col, float ndt, float dz, unsigned mask) {
+  static_assert(CH >= 4, "four halo samples per side");
+  const int lane = threadIdx.x & 31;
+  const int t0 = lane * CH;
+  const bool nf = lane != 0, nl = lane != 31;  // run not at the column start / end
+  const float c = -ndt * dz;
+  auto sl = [](float a, float b, float d) { return kt_slope<MC>(a, b, d); };
+  const float a0 = col.get(t0), a1 = col.get(t0 + 1), a2 = col.get(t0 + 2), a3 = col.get(t0 + 3);
+  const float z0 = col.get(t0 + CH - 4), z1 = col.get(t0 + CH - 3), z2 = col.get(t0 + CH - 2),
+              z3 = col.get(t0 + CH - 1);
+  float hm4 = __shfl_up_sync(mask, z0, 1), hm3 = __shfl_up_sync(mask, z1, 1);
+  float hm2 = __shfl_up_sync(mask, z2, 1), hm1 = __shfl_up_sync(mask, z3, 1);
+  float hp[4] = {__shfl_down_sync(mask, a0, 1), __shfl_down_sync(mask, a1, 1),
+                 __shfl_down_sync(mask, a2, 1), __shfl_down_sync(mask, a3, 1)};
+  if (!nf) hm4 = hm3 = hm2 = hm1 = 0.f;
+  if (!nl) hp[0] = hp[1] = hp[2] = hp[3] = 0.f;
+  // prologue: slopes at t0-3 .. t0+2, fluxes at t0-5/2 .. t0+3/2, s1 at t0-2 .. t0+1
+  const float sm3 = nf ? sl(hm4, hm3, hm2) : 0.f, sm2 = nf ? sl(hm3, hm2, hm1) : 0.f;
+  const float sm1 = nf ? sl(hm2, hm1, a0) : 0.f, s0 = nf ? sl(hm1, a0, a1) : 0.f;
+  float sA = sl(a0, a1, a2), sB = sl(a1, a2, a3);  // slopes at t+1, t+2
+  const float fm25 = kt_fh(hm3 + 0.5f * sm3, hm2 - 0.5f * sm2);
+  const float fm15 = kt_fh(hm2 + 0.5f * sm2, hm1 - 0.5f * sm1);
+  const float fm05 = kt_fh(hm1 + 0.5f * sm1, a0 - 0.5f * s0);
+  const float fp05 = kt_fh(a0 + 0.5f * s0, a1 - 0.5f * sA);
+  float F = kt_fh(a1 + 0.5f * sA, a2 - 0.5f * sB);  // flux at t+3/2
+  const float r_m2 = hm2 + c * (fm15 - fm25);
+  const float r_m1 = hm1 + c * (fm05 - fm15);
+  float r0 = nf ? a0 + c * (fp05 - fm05) : a0;  // s1[t]
+  float r1 = a1 + c * (F - fp05);               // s1[t+1]
+  const float qm1 = nf ? sl(r_m2, r_m1, r0) : 0.f;
+  float q0 = nf ? sl(r_m1, r0, r1) : 0.f;        // slope of s1 at t
+  float G = kt_fh(r_m1 + 0.5f * qm1, r0 - 0.5f * q0);  // flux of s1 at t-1/2
+  float w0 = a0, w1 = a1, w2 = a2, w3 = a3;      // u[t .. t+3]
+#pragma unroll
+  for (int i = 0; i < CH; ++i) {
+    const int t = t0 + i;
+    const float u4 = (i + 4 < CH) ? col.get(t + 4) : hp[(i + 4 - CH) & 3];
+    float sC = sl(w2, w3, u4);                    // slope at t+3
+    if (i >= CH - 4 && !nl) sC = 0.f;             // t+3 >= nT-1
+    const float F2 = kt_fh(w2 + 0.5f * sB, w3 - 0.5f * sC);  // flux at t+5/2
+    float r2 = w2 + c * (F2 - F);                 // s1[t+2]
+    if (i >= CH - 3 && !nl) r2 = w2;              // t+2 >= nT-1 (zero outside)
+    float q1 = sl(r0, r1, r2);                    // slope of s1 at t+1
+    if (i >= CH - 2 && !nl) q1 = 0.f;
+    const float G1 = kt_fh(r0 + 0.5f * q0, r1 - 0.5f * q1);  // flux of s1 at t+1/2
+    float out = 0.5f * w0 + 0.5f * (r0 + c * (G1 - G));
+    if ((i == 0 && !nf) || (i == CH - 1 && !nl)) out = w0;    // column ends
+    col.set(t, out);
+    w0 = w1; w1 = w2; w2 = w3; w3 = u4;
+    sA = sB; sB = sC; F = F2;
+    r0 = r1; r1 = r2; q0 = q1; G = G1;
+  }
+  __syncwarp(mask);
+}
+
 template <class Col>
 ASG_DEV float column_absmax(const Col& col, int nT) {
   const int lane = threadIdx.x & 31;
@@ -366,17 +438,15 @@ ASG_DEV float column_absmax(const Col& col, int nT) {
 // ---------------------------------------------------------------------------
 // The whole column phase.  CH = ceil(nT/32) samples per lane.
 // ---------------------------------------------------------------------------
-// SKEWED: the KT sub-steps (CH <= 32) run on the per-warp skewed copy `skew`.
-template <int CH, bool SKEWED = false, class Col>
+// STREAM: the column holds exactly nT = 32 CH samples (CH >= 4) and the KT
+// sub-steps stream along it in place (kt_step_stream).
+template <int CH, bool STREAM = false, class Col>
 ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const ColumnOps& op,
-                           bool write_stats, float* skew = nullptr) {
+                           bool write_stats) {
   const int lane = threadIdx.x & 31;
   const unsigned mask = 0xffffffffu;
-  // the KT steps on the skewed copy take the taper on the way into it
-  const bool fuse_taper =
-      SKEWED && CH <= 32 && (op.flux == FLUX_KT_MC || op.flux == FLUX_KT_MINMOD);
   // 1) taper
-  if (op.abl_xy != nullptr && !fuse_taper) {
+  if (op.abl_xy != nullptr) {
     const float axy = op.abl_xy[c];
 #pragma unroll
     for (int i = 0; i < CH; ++i) {
@@ -397,25 +467,9 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
     if (op.flux == FLUX_RUSANOV || op.flux == FLUX_RUSANOV_TVD) {
       rusanov_column(col, nT, coef_rus, op.flux == FLUX_RUSANOV_TVD, op.beta_tvd, mask);
     } else {
-      if constexpr (CH <= 32 && SKEWED) {
-        // taper (when fused) and copy into the bank-conflict-free layout
-        const SkewColumn sk{skew};
-        const float axy = op.abl_xy != nullptr ? op.abl_xy[c] : 1.f;
-#pragma unroll
-        for (int i = 0; i < CH; ++i) {
-          const int t = lane + 32 * i;
-          if (t < nT) {
-            const float v = col.get(t);
-            sk.set(t, op.abl_xy != nullptr ? v * (axy * op.abl_t[t]) : v);
-          }
-        }
-        __syncwarp(mask);
-      }
       int nsub = 1;
       if (op.cfl_target > 0.f) {
-        float um;
-        if constexpr (CH <= 32 && SKEWED) um = column_absmax(SkewColumn{skew}, nT);
-        else um = column_absmax(col, nT);
+        const float um = column_absmax(col, nT);
         float cfl = ndt * um * op.dz;
         if (!(cfl <= op.cfl_target || um < 1e-30f)) {
           float q = ceilf(cfl / op.cfl_target);
@@ -429,26 +483,12 @@ ASG_DEV float column_phase(const Col& col, const Col& stg, int c, int nT, const 
         if (op.subcycle_hist != nullptr && lane == 0)
           atomicAdd(op.subcycle_hist + min(nsub, 63), 1u);
       }
-      float dzs = op.dz / (float)nsub;
-      if constexpr (CH <= 32 && SKEWED) {
-        {
-          // sub-steps on the bank-conflict-free copy of the column
-          const SkewColumn sk{skew};
-          for (int k = 0; k < nsub; ++k) {
-            if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(sk, nT, ndt, dzs, mask);
-            else kt_column_step_chunk<CH, false>(sk, nT, ndt, dzs, mask);
-          }
-#pragma unroll
-          for (int i = 0; i < CH; ++i) {
-            const int t = lane + 32 * i;
-            if (t < nT) col.set(t, sk.get(t));
-          }
-          __syncwarp(mask);
-          nsub = 0;
-        }
-      }
+      const float dzs = op.dz / (float)nsub;
       for (int k = 0; k < nsub; ++k) {
-        if constexpr (CH <= 32 && SKEWED) {
+        if constexpr (STREAM) {
+          static_assert(CH >= 4 && CH <= 64, "streamed KT: 128 to 2048 samples");
+          if (op.flux == FLUX_KT_MC) kt_step_stream<CH, true>(col, ndt, dzs, mask);
+          else kt_step_stream<CH, false>(col, ndt, dzs, mask);
         } else if constexpr (CH <= 32) {
           if (op.flux == FLUX_KT_MC) kt_column_step_chunk<CH, true>(col, nT, ndt, dzs, mask);
           else kt_column_step_chunk<CH, false>(col, nT, ndt, dzs, mask);

@@ -34,11 +34,11 @@ ASG_DEFINE_ROOT_UPLOADER(asg_roots_upload_t)
 // ---------------------------------------------------------------------------
 enum TMode : int { TM_PLAIN = 0, TM_FLUX = 1, TM_STATS = 2 };
 
-// Register budget: the KT window of the flux mode needs up to 128 registers
-// (2 blocks per SM); the other modes run 3 blocks per SM with 16 columns or
-// from 512 samples up (shared memory allows no more) and 4 otherwise.
+// Register budget: 3 blocks per SM with 16 columns or from 512 samples up
+// (shared memory allows no more) and 4 otherwise, in every mode (the streamed
+// KT step keeps about 25 values live).
 template <class PL, int MODE, int C>
-__global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 : 2) : ((PL::N >= 512 || C == 16) ? 3 : 4)))
+__global__ void __launch_bounds__(256, ((PL::N >= 512 || C == 16) ? 3 : 4))
     tk_fast(TParams p) {
   if (*p.status != 0) return;
   static_assert(C == 8 || C == 16, "8 or 16 columns per block");
@@ -52,15 +52,12 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
   // different shared-memory banks in the pair (k, M-k) phases
   constexpr int LS = PL::PADDED + 2;
   const int nT = 2 * M;
-  // flux mode: columns up to 1024 samples run the KT sub-steps on one skewed
-  // per-warp copy (SKW floats); longer ones need a stage line per column
-  constexpr bool KT_CHUNK = CH <= 32;
-  constexpr int SKW = skew_floats(2 * M);
-  constexpr int EXTRA = MODE != TM_FLUX ? 0 : (KT_CHUNK ? 8 * SKW / 2 : C * LS);  // float2
+  // flux mode: the KT sub-steps stream along each column in place (every
+  // fast length is a multiple of 32 samples), so no shared memory beyond the
+  // lines is needed
   extern __shared__ float4 smraw[];
   float2* lines = reinterpret_cast<float2*>(smraw);
-  float2* stage = lines + C * LS;                       // TM_FLUX only
-  float2* twM = stage + EXTRA;
+  float2* twM = lines + C * LS;
   const float2* __restrict__ twT = p.tw;                // W_2M^k, k <= M (L1-cached)
   __shared__ float red_max[8];
 
@@ -157,6 +154,21 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
       stepA_inv_smem<PL>(lines + (warp + 8 * j) * LS, b, twM);
     }
     __syncwarp();
+    if (MODE != TM_STATS && p.op.abl_xy != nullptr) {
+      // boundary taper on sample pairs (slot s holds samples 2s, 2s+1)
+      const float2* __restrict__ abl2 = reinterpret_cast<const float2*>(p.op.abl_t);
+#pragma unroll 1
+      for (int j = 0; j < CPW; ++j) {
+        float2* line = lines + (warp + 8 * j) * LS;
+        const float axy = __ldg(p.op.abl_xy + col_of(warp + 8 * j));
+#pragma unroll 4
+        for (int s = lane; s < M; s += 32) {
+          const float2 v = line[PL::pos(s)], w = __ldg(abl2 + s);
+          line[PL::pos(s)] = make_float2(v.x * (axy * w.x), v.y * (axy * w.y));
+        }
+      }
+      __syncwarp();
+    }
   }
 
   // ---------------- phase 2: column work ----------------
@@ -167,14 +179,11 @@ __global__ void __launch_bounds__(256, (MODE == 1 ? (C == 8 && PL::N <= 512 ? 3 
     float2* line = lines + cc * LS;
     const int mycol = col_of(cc);
     PaddedColumn<N2> col{reinterpret_cast<float*>(line)};
-    PaddedColumn<N2> stg{
-        reinterpret_cast<float*>((MODE == TM_FLUX && !KT_CHUNK) ? stage + cc * LS : line)};
-    float* skew = (MODE == TM_FLUX && KT_CHUNK) ? reinterpret_cast<float*>(stage) + warp * SKW
-                                                : nullptr;
     ColumnOps op = p.op;
     if (MODE != TM_FLUX) op.flux = FLUX_NONE;
+    op.abl_xy = nullptr;  // tapered at the end of phase 1
     const float a =
-        column_phase<CH, MODE == TM_FLUX && KT_CHUNK>(col, stg, mycol, nT, op, MODE == TM_STATS, skew);
+        column_phase<CH, MODE == TM_FLUX>(col, col, mycol, nT, op, MODE == TM_STATS);
     am = (a != a || am != am) ? __uint_as_float(0x7fc00000u) : fmaxf(am, a);
     if (p.write_real) {
       float2* dst = reinterpret_cast<float2*>(p.real_out + (size_t)mycol * nT);
@@ -374,9 +383,7 @@ template <int M, int MODE, int C>
 static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   using PL = FastPlan<M>;
   constexpr int LS = PL::PADDED + 2;
-  constexpr bool KT_CHUNK = (2 * M + 31) / 32 <= 32;
-  constexpr int EXTRA = MODE != TM_FLUX ? 0 : (KT_CHUNK ? 8 * skew_floats(2 * M) / 2 : C * LS);
-  const size_t smem = (size_t)(C * LS + EXTRA + M) * sizeof(float2);
+  const size_t smem = (size_t)(C * LS + M) * sizeof(float2);
   static bool attr_done[ASG_MAX_DEVICES] = {};
   const int dev = asg_device_slot();
   if (!attr_done[dev]) {

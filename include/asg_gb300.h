@@ -204,6 +204,9 @@ typedef struct {
                       * barrier in a cooperative launch, which is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
                       * beside other heavy work on the same GPU) */
+  int xy_l2_hint;    /* L2 eviction priority in those kernels: 0 none, 1 the spectrum rows
+                      * streamed from and to HBM evict-first (the group's exchange scratch
+                      * stays in L2), 2 as 1 plus evict-last on the scratch */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of
