@@ -31,7 +31,7 @@ EXPORTED = [
     "asg_net_param_count", "asg_net_create", "asg_net_destroy", "asg_net_set_params",
     "asg_net_get_params", "asg_net_forward", "asg_net_train_step", "asg_flux_columns_learned",
     "asg_net_set_output_scale", "asg_add_source_compact", "asg_debug_set_barrier_skew",
-    "asg_flux_columns_device_clamped",
+    "asg_flux_columns_device_clamped", "asg_set_learned", "asg_learned_stats",
 ]
 KERNEL_KINDS = ["xy_A", "t_nonlin", "xy_B", "t_mid", "xy_C", "t_end", "other"]
 
@@ -74,8 +74,7 @@ _DP = C.POINTER(C.c_double)
 class Tuning(C.Structure):
     _fields_ = [("t_cols_flux", C.c_int), ("t_cols_plain", C.c_int),
                 ("t_cols_stats", C.c_int), ("xy_clusters", C.c_int),
-                ("xy_clusters_closing", C.c_int), ("xy_sync", C.c_int),
-                ("xy_l2_hint", C.c_int)]
+                ("xy_clusters_closing", C.c_int), ("xy_sync", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -126,6 +125,8 @@ def load(require_device: bool = True):
                                             C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, P]
     lib.asg_flux_columns_device_clamped.argtypes = [P, C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
+    lib.asg_set_learned.argtypes = [P, P, C.c_int, C.c_float]
+    lib.asg_learned_stats.argtypes = [P, C.POINTER(C.c_long), C.POINTER(C.c_long)]
     lib.asg_get_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_set_tuning.argtypes = [P, C.POINTER(Tuning)]
     lib.asg_debug_set_barrier_skew.argtypes = [P, C.c_int]

@@ -173,6 +173,36 @@ def training_pairs(cols, n_coef, dz, dt, cfl_target, gamma=1.0, max_sub=4096, mi
     return x, target, mask, coarse, fine
 
 
+def random_focused_field(grid, rng, dX=1.5e-4, dT=1e-8):
+    """One seeded random focused field (peak 0.5-3 MPa, 1-3 MHz, aperture
+    radius 0.25-0.4 of the grid width, focus 15-40 mm, 2-6 cycles) on an
+    (nX, nY, nT) grid; returns (field, f0)."""
+    nX, nY, nT = grid
+    x = (np.arange(nX) - (nX - 1) / 2.0) * dX
+    y = (np.arange(nY) - (nY - 1) / 2.0) * dX
+    t = np.arange(nT) * dT
+    t = t - t.mean()
+    XX, YY = np.meshgrid(x, y, indexing="ij")
+    p0 = rng.uniform(0.5e6, 3e6)
+    f0 = rng.uniform(1e6, 3e6)
+    radius = rng.uniform(0.25, 0.4) * nX * dX
+    focus = rng.uniform(15e-3, 40e-3)
+    ncyc = rng.uniform(2.0, 6.0)
+    r2 = XX ** 2 + YY ** 2
+    ap = r2 <= radius ** 2
+    delay = np.where(ap, r2 / (2 * focus * 1540.0), 0.0)
+    delay = np.where(ap, delay - delay[ap].mean(), 0.0)
+    w0 = 2 * np.pi * f0
+    u0 = np.zeros((nX, nY, nT), np.float32)
+    ix, iy = np.nonzero(ap)
+    for s0 in range(0, ix.size, 4096):  # aperture columns only, in chunks
+        sl = slice(s0, s0 + 4096)
+        tt = t[None, :] + delay[ix[sl], iy[sl]][:, None]
+        u0[ix[sl], iy[sl], :] = (np.exp(-(1.05 * tt * w0 / (ncyc * np.pi)) ** 4)
+                                 * np.sin(w0 * tt) * p0).astype(np.float32)
+    return u0, f0
+
+
 def focused_field_columns(n_fields, grid=(96, 96, 1024), steps=40, seed=0, dX=1.5e-4, dT=1e-8,
                           dz=1e-4, min_frac=0.1):
     """Columns of seeded random focused fields (peak 0.5-3 MPa, 1-3 MHz) after
@@ -181,27 +211,10 @@ def focused_field_columns(n_fields, grid=(96, 96, 1024), steps=40, seed=0, dX=1.
     import torch
     from .solver import SolverParams, angular_spectrum_solve
     rng = np.random.default_rng(seed)
-    nX, nY, nT = grid
-    x = (np.arange(nX) - (nX - 1) / 2.0) * dX
-    y = (np.arange(nY) - (nY - 1) / 2.0) * dX
-    t = np.arange(nT) * dT
-    t = t - t.mean()
-    XX, YY = np.meshgrid(x, y, indexing="ij")
+    nT = grid[2]
     out = []
     for _ in range(n_fields):
-        p0 = rng.uniform(0.5e6, 3e6)
-        f0 = rng.uniform(1e6, 3e6)
-        radius = rng.uniform(0.25, 0.4) * nX * dX
-        focus = rng.uniform(15e-3, 40e-3)
-        ncyc = rng.uniform(2.0, 6.0)
-        r2 = XX ** 2 + YY ** 2
-        ap = r2 <= radius ** 2
-        delay = np.where(ap, r2 / (2 * focus * 1540.0), 0.0)
-        delay = np.where(ap, delay - delay[ap].mean(), 0.0)
-        w0 = 2 * np.pi * f0
-        tt = t[None, None, :] + delay[:, :, None]
-        u0 = (np.exp(-(1.05 * tt * w0 / (ncyc * np.pi)) ** 4) * np.sin(w0 * tt) * p0
-              * ap[:, :, None]).astype(np.float32)
+        u0, f0 = random_focused_field(grid, rng, dX, dT)
         prm = SolverParams(dX=dX, dY=dX, dT=dT, c0=1540.0, rho0=1000.0, beta=3.5, alpha0=0.5,
                            attenPow=1.0, f0=f0, propDist=steps * dz, dZmin=dz, fluxScheme="kt")
         field = angular_spectrum_solve(u0, prm, verbose=False)[0]

@@ -208,7 +208,6 @@ struct asg_plan {
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
-  int l2_hint = 0;            // L2 eviction priorities of the L2 plane kernels (0, 1, 2)
   int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
                               // 1 thread-block cluster, 2 counters in a cooperative launch
   int batch_refs = 0;         // batches holding the plan (they use cluster barriers)
@@ -230,6 +229,13 @@ struct asg_plan {
   cudaEvent_t ev0, ev1;
   float2* spec = nullptr;
   float* real = nullptr;
+  // learned KT stage (asg_set_learned): the network, its gate, the second real
+  // buffer and the counts of the last run
+  asg_net* learned_net = nullptr;
+  int learned_min_sub = 0;
+  float learned_shock = 0.f;
+  float* real2 = nullptr;
+  long learned_cols = 0, learned_col_steps = 0;
   float2 *twT = nullptr, *twM = nullptr, *twX = nullptr, *twY = nullptr;
   int *f_of_plane = nullptr, *cls_x = nullptr, *cls_y = nullptr;
   int ncx, ncy;
@@ -343,7 +349,7 @@ extern "C" int asg_plan_destroy(asg_plan* p) {
     cudaFree(s.val);
   }
   if (p->step_graph) cudaGraphExecDestroy(p->step_graph);
-  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->grp_cnt, p->spec, p->spec2, p->nyq_tmp, p->real, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
+  void* ptrs[] = {p->l2_scratch, p->l2_cls_x, p->grp_cnt, p->spec, p->spec2, p->nyq_tmp, p->real, p->real2, p->twT, p->twM, p->twX, p->twY, p->f_of_plane, p->cls_x,
                   p->cls_y, p->kx2, p->ky2, p->tab_scratch, p->abl_xy_half, p->abl_t_half,
                   p->abl_xy_full, p->abl_t_full, p->fw_lx, p->fw_ly, p->fw_exp, p->sa_wx,
                   p->sa_wy, p->sa_coef, p->screen_fscale, p->obl_tab, p->power_acc,
@@ -906,7 +912,6 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
                           ? p->xy_clusters : L2_MAX_CLUSTERS;
   x.coop = xy_sync_of(p) == 2 ? 1 : 0;
-  x.l2_hint = p->l2_hint;
   x.grp_cnt = p->grp_cnt;
   x.grp_skew = p->barrier_skew;
   x.spec_tmp = p->spec2;
@@ -955,6 +960,38 @@ static int nonlinear_stage(asg_plan* p, double dz, double beta_tvd, const float*
     TParams t = tparams(p);
     t.op.abl_xy = axy;
     t.op.abl_t = at;
+    t.do_r2c = 1;
+    return run_t(p, t, ASG_K_T_NONLIN);
+  }
+  if (p->learned_net != nullptr && !p->cfg.nonlinear_obliquity &&
+      (flux == ASG_FLUX_KT || flux == ASG_FLUX_KT_MINMOD)) {
+    // learned KT stage: (1) inverse transform and taper into real columns,
+    // (2) per column the gated learned step (one coarse KT step plus the
+    // network's correction) or the plain sub-cycled KT step as its fallback,
+    // (3) forward transform of the result
+    {
+      TParams t = tparams(p);
+      t.op.abl_xy = axy;
+      t.op.abl_t = at;
+      t.write_real = 1;
+      t.real_out = p->real;
+      t.do_r2c = 0;
+      CKS(run_t(p, t, ASG_K_T_NONLIN));
+    }
+    {
+      KScope k(p, ASG_K_T_NONLIN);
+      int nl = 0;
+      const int s = asg_flux_columns_learned(
+          p->learned_net, p->real, p->real2, p->ncols, p->T, flux, p->N, dz, p->cfg.dT,
+          p->cfg.kt_cfl_target, p->cfg.kt_max_subcycles > 0 ? p->cfg.kt_max_subcycles : 1024,
+          p->learned_min_sub, p->learned_shock, &nl, p->st);
+      if (s != ASG_OK) return s;
+      p->learned_cols += nl;
+      p->learned_col_steps += p->ncols;
+    }
+    TParams t = tparams(p);
+    t.in_real = 1;
+    t.real_in = p->real2;
     t.do_r2c = 1;
     return run_t(p, t, ASG_K_T_NONLIN);
   }
@@ -1234,6 +1271,7 @@ static int prepare_run(asg_plan* p, const float* init, double prop_dist, double 
     CK(cudaMemsetAsync(p->d_step, 0, sizeof(int), p->st));
   }
   p->zaxis.clear();
+  p->learned_cols = p->learned_col_steps = 0;
   for (int i = 0; i < ASG_NKINDS; ++i) {
     p->launches[i] = 0;
     p->kms[i] = 0.0;
@@ -1246,6 +1284,7 @@ static int prepare_run(asg_plan* p, const float* init, double prop_dist, double 
 // source crossing, not the last, no callback, profiling off.
 static bool step_is_regular(const asg_plan* p, const RunState& rs, size_t k, bool has_cb) {
   if (!p->use_graphs || has_cb || p->prof || k + 1 == rs.steps.size()) return false;
+  if (p->learned_net != nullptr) return false;  // the learned stage reads a count on the host
   const double dzs = rs.steps[k], z = rs.zbefore[k];
   if (fabs(dzs - rs.dz) > 1e-15) return false;
   for (auto& sc : p->screens)
@@ -1636,7 +1675,6 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   ncl = p->xy_clusters_c > 0 ? p->xy_clusters_c : L2_MAX_CLUSTERS;
   out->xy_clusters_closing = p->l2 ? ncl : 0;
   out->xy_sync = xy_sync_of(p);
-  out->xy_l2_hint = p->l2 ? p->l2_hint : 0;
   return ASG_OK;
 }
 
@@ -1655,13 +1693,10 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
     return fail(ASG_ERR_ARG, "cluster caps %d, %d outside 0..%d", t->xy_clusters,
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
   if (t->xy_sync < 0 || t->xy_sync > 2) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..2", t->xy_sync);
-  if (t->xy_l2_hint < 0 || t->xy_l2_hint > 2)
-    return fail(ASG_ERR_ARG, "xy_l2_hint %d outside 0..2", t->xy_l2_hint);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
   p->xy_sync = t->xy_sync;
-  p->l2_hint = t->xy_l2_hint;
   p->gen++;
   return ASG_OK;
 }
@@ -1739,25 +1774,6 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
     }
     p->xy_clusters = best_n;
   }
-  if (p->l2 && status == ASG_OK) {
-    // L2 eviction priorities: the plain diffraction pass and the closing pass together
-    const bool closing = p->cfg.freq_weighted || p->cfg.super_absorbing;
-    double best = 1e300;
-    int best_h = 0;
-    for (int h : {0, 1, 2}) {
-      p->l2_hint = h;
-      double ms = 0.0, ms_c = 0.0;
-      status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);
-      if (status != ASG_OK) break;
-      if (closing)
-        ms_c = p->launches[ASG_K_XY_C] > 0 ? p->kms[ASG_K_XY_C] / p->launches[ASG_K_XY_C] : 0.0;
-      if (ms + ms_c < best) {
-        best = ms + ms_c;
-        best_h = h;
-      }
-    }
-    p->l2_hint = best_h;
-  }
   // the closing-stage kernel runs when the step has a boundary epilogue
   if (p->l2 && (p->cfg.freq_weighted || p->cfg.super_absorbing) && status == ASG_OK) {
     double best = 1e300;
@@ -1778,6 +1794,37 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
   p->gen++;
   if (status != ASG_OK) return status;
   return chosen ? asg_get_tuning(p, chosen) : ASG_OK;
+}
+
+extern "C" int asg_set_learned(asg_plan* p, asg_net* net, int min_subcycles,
+                               float shock_ratio) {
+  g_err.clear();
+  if (!p) return fail(ASG_ERR_ARG, "null argument");
+  if (net == nullptr) {
+    p->learned_net = nullptr;
+    return ASG_OK;
+  }
+  if (!(p->cfg.kt_cfl_target > 0.0))
+    return fail(ASG_ERR_STATE, "the learned KT stage needs per-column sub-cycling "
+                               "(kt_cfl_target > 0): it defines the gate and the fallback");
+  if (p->cfg.flux != ASG_FLUX_KT && p->cfg.flux != ASG_FLUX_KT_MINMOD)
+    return fail(ASG_ERR_ARG, "the learned step corrects the KT schemes only");
+  if (p->T % 128 != 0 || p->T > 1024)
+    return fail(ASG_ERR_SHAPE, "learned step: nT a multiple of 128 up to 1024 (nT=%d)", p->T);
+  if (min_subcycles < 1) return fail(ASG_ERR_ARG, "min_subcycles < 1");
+  if (!p->real2) CKS(dalloc(&p->real2, (size_t)p->ncols * p->T));
+  p->learned_net = net;
+  p->learned_min_sub = min_subcycles;
+  p->learned_shock = shock_ratio;
+  p->gen++;
+  return ASG_OK;
+}
+
+extern "C" int asg_learned_stats(asg_plan* p, long* learned_columns, long* column_steps) {
+  if (!p) return fail(ASG_ERR_ARG, "null argument");
+  if (learned_columns) *learned_columns = p->learned_cols;
+  if (column_steps) *column_steps = p->learned_col_steps;
+  return ASG_OK;
 }
 
 extern "C" int asg_debug_set_barrier_skew(asg_plan* p, int skew) {

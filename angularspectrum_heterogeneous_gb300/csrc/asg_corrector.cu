@@ -21,6 +21,7 @@
 // The 64x64 layers are GEMMs with M = 64 output channels, N = positions,
 // K = 5 taps x 64 input channels, issued as mma.sync.m16n8k16 BF16 tiles.
 #include <math.h>
+#include <stdio.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -833,7 +834,7 @@ static int net_ensure_inf(asg_net* n, size_t ncols, int nT) {
   const size_t chunk = npos < INF_CHUNK_POS ? npos : INF_CHUNK_POS;
   bool ok = cudaMalloc(&n->inf_x, npos * 4) == cudaSuccess &&
             cudaMalloc(&n->inf_s, ncols * 4) == cudaSuccess &&
-            cudaMalloc(&n->inf_col, (ncols + 1) * 4) == cudaSuccess &&
+            cudaMalloc(&n->inf_col, (ncols + 4) * 4) == cudaSuccess &&
             cudaMalloc(&n->inf_y, chunk * 4) == cudaSuccess &&
             cudaMalloc(&n->inf_a, chunk * NCH * 2) == cudaSuccess &&
             cudaMalloc(&n->inf_b, chunk * NCH * 2) == cudaSuccess;
@@ -1105,6 +1106,7 @@ struct GateParams {
   int* list_col;      // [ncols]
   float* list_s;      // [ncols] output scale of each learned column
   int* counter;       // learned columns so far (starts at zero)
+  unsigned* clamp;    // [2] fallback columns capped at max_sub, largest count needed
 };
 
 template <int CH>
@@ -1136,6 +1138,14 @@ __global__ void __launch_bounds__(256) k_flux_gate(GateParams p) {
     }
   }
   const bool learned = nsub >= p.min_sub && steep <= p.shock_ratio * s && s > 1e-30f;
+  if (!learned && lane == 0 && p.cfl_target > 0.f) {
+    // a fallback column capped at max_sub sub-cycles runs above its CFL target
+    const float q = ceilf(p.ndt * s * p.dz / p.cfl_target);
+    if (q > (float)p.max_sub) {
+      atomicAdd(p.clamp, 1u);
+      atomicMax(p.clamp + 1, q < 4.0e9f ? (unsigned)q : 0xffffffffu);
+    }
+  }
   const int steps = learned ? 1 : nsub;
   const float dzs = p.dz / (float)steps;
   for (int k = 0; k < steps; ++k) {
@@ -1205,8 +1215,8 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
   float* xrows = n->inf_x;
   int* list_col = n->inf_col;
   float* list_s = n->inf_s;
-  int* counter = n->inf_col + ncols;
-  if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess)
+  int* counter = n->inf_col + ncols;  // then the two sub-cycle cap counters
+  if (cudaMemsetAsync(counter, 0, 3 * sizeof(int), st) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "counter reset");
   GateParams g;
   g.in = d_in;
@@ -1226,15 +1236,17 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
   g.list_col = list_col;
   g.list_s = list_s;
   g.counter = counter;
+  g.clamp = reinterpret_cast<unsigned*>(counter + 1);
   const int ch = (nT + 31) / 32;
   const int s = ch <= 2 ? launch_gate<2>(g, st) : ch <= 4 ? launch_gate<4>(g, st)
               : ch <= 8 ? launch_gate<8>(g, st) : ch <= 16 ? launch_gate<16>(g, st)
               : launch_gate<32>(g, st);
   if (s != ASG_OK) return net_fail(s, "gate launch");
-  int k = 0;
-  if (cudaMemcpyAsync(&k, counter, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+  int cnt[3] = {0, 0, 0};
+  if (cudaMemcpyAsync(cnt, counter, sizeof(cnt), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return net_fail(ASG_ERR_CUDA, "learned-column count");
+  const int k = cnt[0];
   if (n_learned) *n_learned = k;
   const int rows_per_chunk = (int)(INF_CHUNK_POS / (size_t)nT);
   for (int r0 = 0; r0 < k; r0 += rows_per_chunk) {
@@ -1244,5 +1256,13 @@ extern "C" int asg_flux_columns_learned(asg_net* n, const float* d_in, float* d_
     if (cudaPeekAtLastError() != cudaSuccess) return net_fail(ASG_ERR_CUDA, "apply launch");
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return net_fail(ASG_ERR_CUDA, "learned step");
-  return net_check_tc(n);
+  CKS_NET(net_check_tc(n));
+  if (cnt[1] != 0) {
+    char msg[200];
+    snprintf(msg, sizeof msg,
+             "%u fallback columns needed more KT sub-cycles than the cap of %d (up to %u) and "
+             "ran above the CFL target", (unsigned)cnt[1], g.max_sub, (unsigned)cnt[2]);
+    return net_fail(ASG_ERR_SUBCYCLES, msg);
+  }
+  return ASG_OK;
 }

@@ -102,7 +102,6 @@ struct XYParams {
   unsigned grp_skew;       // added to every barrier target (test hook: 0 in normal runs)
   float2* spec_tmp;        // [planes][X][Y] work spectrum of the large generic planes
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
-  int l2_hint;             // L2 eviction priorities of the L2-exchange kernels (0, 1, 2)
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);

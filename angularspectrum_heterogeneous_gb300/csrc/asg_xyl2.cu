@@ -35,45 +35,6 @@ ASG_DEV void cp_async16(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
-
-// L2 eviction priority of the plane kernels' global traffic (XYParams::l2_hint):
-// 0 none; 1 the spectrum rows streamed from and to HBM are evict-first, so that
-// the group's exchange scratch stays in L2 while the spectrum streams through;
-// 2 as 1, and the scratch accesses are evict-last.
-struct L2Hints {
-  uint64_t stream, scratch;
-  bool on_stream, on_scratch;
-};
-ASG_DEV L2Hints make_l2_hints(int mode) {
-  L2Hints h;
-  h.on_stream = mode >= 1;
-  h.on_scratch = mode >= 2;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(h.stream));
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(h.scratch));
-  return h;
-}
-ASG_DEV void cp_async16_hint(void* smem, const void* gmem, bool on, uint64_t pol) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  if (on)
-    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(sa),
-                 "l"(gmem), "l"(pol) : "memory");
-  else
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-ASG_DEV void st_hint(float2* g, float2 v, bool on, uint64_t pol) {
-  if (on)
-    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(g), "f"(v.x),
-                 "f"(v.y), "l"(pol) : "memory");
-  else
-    *g = v;
-}
-ASG_DEV void st_hint4(float4* g, float4 v, bool on, uint64_t pol) {
-  if (on)
-    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(g),
-                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol) : "memory");
-  else
-    *g = v;
-}
 ASG_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 ASG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -188,7 +149,6 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   for (int i = tid; i < Xs; i += NT) tw_x[i] = p.twX[i * nsub];  // W_Xs^i
   for (int i = tid; i < nsub * Xs; i += NT) clsx[i] = p.l2_cls_x[i];
   float2* scratch0 = p.l2_scratch + (size_t)cid * 2 * Xs * Y;
-  const L2Hints hint = make_l2_hints(p.l2_hint);
 
   auto zero_plane = [&](int q) {
     return p.zero_dc_nyq && is_dc_or_nyq_l2(p.f_of_plane[q / nsub], p.nT);
@@ -200,8 +160,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   auto prefetch_row = [&](int q, int r) {
     const float2* g = sub_base(q) + (size_t)(rank * R + r) * Y;
     float2* d = buf + r * RS;
-    for (int s2 = lane; s2 < Y / 2; s2 += 32)
-      cp_async16_hint(d + PY::pos(2 * s2), g + 2 * s2, hint.on_stream, hint.stream);
+    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
   };
   int issued = -1;
 
@@ -242,8 +201,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       const float2* row = buf + r * RS;
       float4* dst = reinterpret_cast<float4*>(S + (size_t)(rank * R + r) * Y);
       for (int s2 = lane; s2 < Y / 2; s2 += 32)
-        st_hint4(dst + s2, *reinterpret_cast<const float4*>(row + PY::pos(2 * s2)),
-                 hint.on_scratch, hint.scratch);
+        dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
     }
     // the barrier (release / acquire) orders these global writes before the
     // other CTAs' reads of the scratch
@@ -255,8 +213,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       // tile[x][c], row stride TS
       for (int i = tid; i < Xs * Yc / 2; i += NT) {
         const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
-        cp_async16_hint(buf + x * TS + c2, S + (size_t)x * Y + c0 + c2, hint.on_scratch,
-                        hint.scratch);
+        cp_async16(buf + x * TS + c2, S + (size_t)x * Y + c0 + c2);
       }
       cp_async_commit();
       cp_async_wait_all();
@@ -344,9 +301,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       __syncthreads();
       for (int i = tid; i < Xs * Yc / 2; i += NT) {
         const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
-        st_hint4(reinterpret_cast<float4*>(S + (size_t)x * Y + c0 + c2),
-                 *reinterpret_cast<const float4*>(buf + x * TS + c2), hint.on_scratch,
-                 hint.scratch);
+        *reinterpret_cast<float4*>(S + (size_t)x * Y + c0 + c2) =
+            *reinterpret_cast<const float4*>(buf + x * TS + c2);
       }
     }
     if (!gsync()) break;
@@ -359,8 +315,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       const int r = warp + NW * j;
       const float2* srcr = S + (size_t)(rank * R + r) * Y;
       float2* row = buf + r * RS;
-      for (int s2 = lane; s2 < Y / 2; s2 += 32)
-        cp_async16_hint(row + PY::pos(2 * s2), srcr + 2 * s2, hint.on_scratch, hint.scratch);
+      for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(row + PY::pos(2 * s2), srcr + 2 * s2);
     }
     cp_async_commit();
     int qn = q + ncl;
@@ -385,7 +340,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int ka = 1; ka < PY::N1; ++ka) v[ka] = cmulc(row[PY::pos(b + PY::N2 * ka)], tw_y[b * ka]);
       dft<PY::N1, true>(v);
 #pragma unroll
-      for (int a = 0; a < PY::N1; ++a) st_hint(grow + b + PY::N2 * a, v[a], hint.on_stream, hint.stream);
+      for (int a = 0; a < PY::N1; ++a) grow[b + PY::N2 * a] = v[a];
     }
     __syncwarp();
     if (pref) {
@@ -484,15 +439,13 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
     wxs[i] = (p.epi & EPI_SUPERABS) ? p.sa_wx[i] : 0.f;
   }
   float2* S = p.l2_scratch + (size_t)cid * X * Y;     // rows of a, then rows of b
-  const L2Hints hint = make_l2_hints(p.l2_hint);
   const bool fw = (p.epi & EPI_FREQW) != 0, sa = (p.epi & EPI_SUPERABS) != 0;
   const float st = p.sa_strength;
 
   auto prefetch_row = [&](int plane, int h, int r) {
     const float2* g = p.spec + ((size_t)plane * X + (size_t)h * Xs + rank * R + r) * Y;
     float2* d = buf + r * RS;
-    for (int s2 = lane; s2 < Y / 2; s2 += 32)
-      cp_async16_hint(d + PY::pos(2 * s2), g + 2 * s2, hint.on_stream, hint.stream);
+    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
   };
   int issued = -1;
 
@@ -533,8 +486,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         const float2* row = buf + r * RS;
         float4* dst = reinterpret_cast<float4*>(S + (size_t)(h * Xs + rank * R + r) * Y);
         for (int s2 = lane; s2 < Y / 2; s2 += 32)
-          st_hint4(dst + s2, *reinterpret_cast<const float4*>(row + PY::pos(2 * s2)),
-                   hint.on_scratch, hint.scratch);
+          dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
       }
       __syncwarp();  // my rows are reloaded next
     }
@@ -547,8 +499,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
       float2* tile = buf;  // [h][x][c], h-stride Xs*TS
       for (int i = tid; i < 2 * Xs * YR / 2; i += NT) {
         const int hx = i / (YR / 2), c2 = 2 * (i - hx * (YR / 2));
-        cp_async16_hint(tile + hx * TS + c2, S + (size_t)hx * Y + c0 + c2, hint.on_scratch,
-                        hint.scratch);
+        cp_async16(tile + hx * TS + c2, S + (size_t)hx * Y + c0 + c2);
       }
       cp_async_commit();
       cp_async_wait_all();
@@ -651,9 +602,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
       }
       for (int i = tid; i < 2 * Xs * YR / 2; i += NT) {
         const int hx = i / (YR / 2), c2 = 2 * (i - hx * (YR / 2));
-        st_hint4(reinterpret_cast<float4*>(S + (size_t)hx * Y + c0 + c2),
-                 *reinterpret_cast<const float4*>(tile + hx * TS + c2), hint.on_scratch,
-                 hint.scratch);
+        *reinterpret_cast<float4*>(S + (size_t)hx * Y + c0 + c2) =
+            *reinterpret_cast<const float4*>(tile + hx * TS + c2);
       }
       __syncthreads();  // tile reused by the next round
     }
@@ -668,7 +618,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         const float2* srcr = S + (size_t)(h * Xs + rank * R + r) * Y;
         float2* row = buf + r * RS;
         for (int s2 = lane; s2 < Y / 2; s2 += 32)  // cp.async.cg reads L2: other CTAs wrote these
-          cp_async16_hint(row + PY::pos(2 * s2), srcr + 2 * s2, hint.on_scratch, hint.scratch);
+          cp_async16(row + PY::pos(2 * s2), srcr + 2 * s2);
       }
       cp_async_commit();
       cp_async_wait_all();
@@ -690,7 +640,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         const float2* row = buf + r * RS;
         float2* grow = p.spec + ((size_t)plane * X + x) * Y;
         if (!epi) {
-          for (int y = lane; y < Y; y += 32) st_hint(grow + y, row[PY::pos(y)], hint.on_stream, hint.stream);
+          for (int y = lane; y < Y; y += 32) grow[y] = row[PY::pos(y)];
           continue;
         }
         float2 prev_last = make_float2(0.f, 0.f);  // value at y0-1 (damped, not corrected)
@@ -736,7 +686,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
               res = cscale(res, exp2f(fs * log2f(a)));
             }
           }
-          st_hint(grow + y, res, hint.on_stream, hint.stream);
+          grow[y] = res;
         }
       }
       __syncwarp();

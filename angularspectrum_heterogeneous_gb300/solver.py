@@ -240,6 +240,22 @@ class Plan:
         _lib.check(self.lib.asg_last_run_ms(self.h, C.byref(v)))
         return v.value
 
+    def set_learned(self, net, min_subcycles: int = 10, shock_ratio: float = 0.5):
+        """Learned KT stage (see asg_set_learned): per column one coarse KT step
+        plus the network's correction where the plain step would need at least
+        `min_subcycles` sub-cycles and the column is smooth, the plain
+        sub-cycled KT step elsewhere.  `net` is a corrector.Corrector (kept
+        alive by the plan); None switches the stage off."""
+        _lib.check(self.lib.asg_set_learned(self.h, None if net is None else net.h,
+                                            int(min_subcycles), float(shock_ratio)))
+        self._learned_net = net
+
+    def learned_stats(self):
+        """(columns that took the learned path, column steps) of the last run."""
+        a, b = C.c_long(0), C.c_long(0)
+        _lib.check(self.lib.asg_learned_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def set_graphs(self, enable: bool):
         """Replay regular march steps from one captured CUDA graph (default on)."""
         _lib.check(self.lib.asg_set_graphs(self.h, int(enable)))
@@ -327,6 +343,22 @@ class Batch:
         h = C.c_void_p()
         _lib.check(self.lib.asg_batch_create(arr, len(self.plans), C.byref(h)))
         self.h = h
+
+    def set_learned(self, net, min_subcycles: int = 10, shock_ratio: float = 0.5):
+        """Learned KT stage (see asg_set_learned): per column one coarse KT step
+        plus the network's correction where the plain step would need at least
+        `min_subcycles` sub-cycles and the column is smooth, the plain
+        sub-cycled KT step elsewhere.  `net` is a corrector.Corrector (kept
+        alive by the plan); None switches the stage off."""
+        _lib.check(self.lib.asg_set_learned(self.h, None if net is None else net.h,
+                                            int(min_subcycles), float(shock_ratio)))
+        self._learned_net = net
+
+    def learned_stats(self):
+        """(columns that took the learned path, column steps) of the last run."""
+        a, b = C.c_long(0), C.c_long(0)
+        _lib.check(self.lib.asg_learned_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_graphs(self, enable: bool):
         _lib.check(self.lib.asg_batch_set_graphs(self.h, int(enable)))

@@ -204,9 +204,6 @@ typedef struct {
                       * barrier in a cooperative launch, which is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
                       * beside other heavy work on the same GPU) */
-  int xy_l2_hint;    /* L2 eviction priority in those kernels: 0 none, 1 the spectrum rows
-                      * streamed from and to HBM evict-first (the group's exchange scratch
-                      * stays in L2), 2 as 1 plus evict-last on the scratch */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of
@@ -306,6 +303,19 @@ int asg_flux_columns_learned(asg_net* net, const float* d_in, float* d_out, int 
                              int flux, double n_coef, double dz, double dt, double cfl_target,
                              int max_subcycles, int min_subcycles, float shock_ratio,
                              int* n_learned, void* stream);
+
+/* Learned KT stage in the march (no counterpart in the reference): with a
+ * network set, the nonlinear stage of every step takes, per column, the gated
+ * learned step of asg_flux_columns_learned (one coarse KT step plus the
+ * network's correction where the plain step would need at least min_subcycles
+ * sub-cycles and the column is smooth: max|u[t+1]-u[t]| <= shock_ratio max|u|),
+ * and the plain KT step sub-cycled at the plan's kt_cfl_target elsewhere (its
+ * fallback).  Needs kt_cfl_target > 0, a KT flux and nT a multiple of 128 up to
+ * 1024; steps then launch eagerly (the gate's count is read on the host).  The
+ * net must outlive the plan's runs; NULL switches the stage off. */
+int asg_set_learned(asg_plan* plan, asg_net* net, int min_subcycles, float shock_ratio);
+/* Columns that took the learned path, and column steps in all, of the last run. */
+int asg_learned_stats(asg_plan* plan, long* learned_columns, long* column_steps);
 
 /* Message of the last error on this thread. */
 const char* asg_last_error(void);

@@ -101,6 +101,10 @@ class OracleParams:
     useNonlinearityObliquity: bool = False
     phaseScreens: object = None
     sourcePlanes: object = None
+    # Extension, not a reference field: > 0 sub-cycles the KT step per (x, y)
+    # column at this CFL target (flux_kt_percolumn), the semantics of the GPU
+    # path's per-column mode and of the plain fallback of its learned stage.
+    kt_cfl_target: float = 0.0
 
 
 # ---------------------------------------------------------------------------
@@ -493,13 +497,19 @@ def flux_kt_percolumn(u, N, dZ, dT, cfl_target=0.5):
     cols = u.reshape(-1, shp[-1])
     out = np.empty_like(cols)
     umax = np.max(np.abs(cols), axis=1)
+    nsub = np.ones(cols.shape[0], np.int64)
     for i in range(cols.shape[0]):
         cfl = N * float(umax[i]) * dZ / dT
-        n = 1 if (cfl <= cfl_target or umax[i] < 1e-30) else int(math.ceil(cfl / cfl_target))
-        c = cols[i:i + 1]
-        for _ in range(n):
-            c = flux_kt(c, N, dZ / n, dT)
-        out[i] = c[0]
+        if not (cfl <= cfl_target or umax[i] < 1e-30):
+            nsub[i] = int(math.ceil(cfl / cfl_target))
+    # columns with the same count step together (each column's arithmetic is
+    # its own, so this equals stepping them one by one)
+    for n in np.unique(nsub):
+        sel = np.nonzero(nsub == n)[0]
+        c = cols[sel]
+        for _ in range(int(n)):
+            c = flux_kt(c, N, dZ / int(n), dT)
+        out[sel] = c
     return out.reshape(shp)
 
 
@@ -581,7 +591,9 @@ def solve(initial_field, p: OracleParams, precision="fp32", per_step_callback=No
             u = attenuation_step(u, so["afilt_half"])
             u = diffraction_step(u, so["HH_half"], so["abl_half"])
             Nn = Neff(u)
-            if p.fluxScheme == "kt":
+            if p.fluxScheme == "kt" and p.kt_cfl_target > 0:
+                u = flux_kt_percolumn(u, Nn, dzs, p.dT, p.kt_cfl_target)
+            elif p.fluxScheme == "kt":
                 u = flux_kt(u, Nn, dzs, p.dT)
             elif p.useTVD:
                 beta_tvd = max(1.0, 2.0 - p.adaptiveFilterStrength * (dzs / (c0 / p.f0)) * 10)

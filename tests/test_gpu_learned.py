@@ -79,3 +79,53 @@ def test_gate_selects_the_columns_it_should(trained):
     # columns clearly on the fallback side of the gate (away from its edges)
     plain = (nsub < min_sub - 1) | (steep > 1.01 * ratio * s)
     assert bool((out[plain] == fine[plain]).all())
+
+
+def test_learned_stage_in_the_march(trained):
+    """The learned stage inside the march (asg_set_learned): a 64x64x512
+    focused-piston march of 2 mm KT steps whose focal columns need 10-30
+    sub-cycles at CFL 0.01.  The plain march sub-cycles every column (its
+    FP64 oracle does the same, flux_kt_percolumn); the learned march takes
+    one coarse step plus the network's correction on the columns the gate
+    selects.  Its pnp/ppp/pI stay within 1e-3 of both; their distances from
+    the plain march are printed beside those of the coarse march (one KT
+    step per column, no sub-cycling)."""
+    import oracle.asm_oracle as O
+    import scenarios as S
+    from angularspectrum_heterogeneous_gb300 import Plan
+    from gpu_helpers import oracle_params, rel, solver_params
+    CR, net, held, hist = trained
+    nX, nY, nT = 64, 64, 512
+    kw = dict(dX=1.5e-4, dY=1.5e-4, dT=DT, c0=1540.0, rho0=1000.0, beta=3.5, alpha0=0.5,
+              attenPow=1.0, f0=2e6, dZmin=DZ, propDist=6 * DZ, fluxScheme="kt",
+              stabilityThreshold=1.0)
+    u0 = S.piston_field(nX, nY, nT, kw["dX"], kw["dY"], kw["dT"], kw["f0"], 1.5e6,
+                        radius=0.35 * nX * kw["dX"], focus=10e-3)
+
+    def march(cfl, learned):
+        plan = Plan((nX, nY, nT), solver_params(kw), kt_cfl_target=cfl)
+        try:
+            plan.set_operators(0, DZ)
+            if learned:
+                plan.set_learned(net, min_subcycles=MIN_SUB, shock_ratio=0.5)
+            plan.run(u0, kw["propDist"], DZ)
+            return plan.outputs(), plan.learned_stats()
+        finally:
+            plan.close()
+
+    plain, _ = march(CFL, False)
+    learned, (nl, ncs) = march(CFL, True)
+    coarse, _ = march(0.0, False)
+    assert nl > 0 and ncs == 6 * nX * nY, (nl, ncs)
+    ref = O.solve(u0, oracle_params(dict(kw, kt_cfl_target=CFL)), "fp64")
+    errs = {}
+    for i, k in [(0, "field"), (1, "pnp"), (2, "ppp"), (3, "pI")]:
+        errs[k] = dict(plain_vs_fp64=rel(plain[i], ref[i]), learned_vs_plain=rel(learned[i], plain[i]),
+                       learned_vs_fp64=rel(learned[i], ref[i]), coarse_vs_plain=rel(coarse[i], plain[i]))
+    print(f"\n{nl} learned column steps of {ncs}:",
+          {k: {a: f"{b:.2e}" for a, b in v.items()} for k, v in errs.items()})
+    for k, e in errs.items():
+        bar = 1e-4 if k == "field" else 1e-3
+        assert e["plain_vs_fp64"] < bar, (k, e)
+        if k != "field":
+            assert e["learned_vs_plain"] < 1e-3 and e["learned_vs_fp64"] < 1e-3, (k, e)
