@@ -173,10 +173,10 @@ def training_pairs(cols, n_coef, dz, dt, cfl_target, gamma=1.0, max_sub=4096, mi
     return x, target, mask, coarse, fine
 
 
-def random_focused_field(grid, rng, dX=1.5e-4, dT=1e-8):
+def random_focused_field(grid, rng, dX=1.5e-4, dT=1e-8, focus_range=(15e-3, 40e-3)):
     """One seeded random focused field (peak 0.5-3 MPa, 1-3 MHz, aperture
-    radius 0.25-0.4 of the grid width, focus 15-40 mm, 2-6 cycles) on an
-    (nX, nY, nT) grid; returns (field, f0)."""
+    radius 0.25-0.4 of the grid width, focus drawn from focus_range, 2-6
+    cycles) on an (nX, nY, nT) grid; returns (field, f0)."""
     nX, nY, nT = grid
     x = (np.arange(nX) - (nX - 1) / 2.0) * dX
     y = (np.arange(nY) - (nY - 1) / 2.0) * dX
@@ -186,7 +186,7 @@ def random_focused_field(grid, rng, dX=1.5e-4, dT=1e-8):
     p0 = rng.uniform(0.5e6, 3e6)
     f0 = rng.uniform(1e6, 3e6)
     radius = rng.uniform(0.25, 0.4) * nX * dX
-    focus = rng.uniform(15e-3, 40e-3)
+    focus = rng.uniform(*focus_range)
     ncyc = rng.uniform(2.0, 6.0)
     r2 = XX ** 2 + YY ** 2
     ap = r2 <= radius ** 2

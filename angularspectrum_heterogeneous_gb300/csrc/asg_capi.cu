@@ -208,6 +208,7 @@ struct asg_plan {
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
+  int xy_bulk = 1;            // HBM row loads of the L2 plane kernels (XYParams::bulk_rows)
   int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
                               // 1 thread-block cluster, 2 counters in a cooperative launch
   int batch_refs = 0;         // batches holding the plan (they use cluster barriers)
@@ -912,6 +913,7 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
                           ? p->xy_clusters : L2_MAX_CLUSTERS;
   x.coop = xy_sync_of(p) == 2 ? 1 : 0;
+  x.bulk_rows = p->xy_bulk;
   x.grp_cnt = p->grp_cnt;
   x.grp_skew = p->barrier_skew;
   x.spec_tmp = p->spec2;
@@ -1675,6 +1677,7 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   ncl = p->xy_clusters_c > 0 ? p->xy_clusters_c : L2_MAX_CLUSTERS;
   out->xy_clusters_closing = p->l2 ? ncl : 0;
   out->xy_sync = xy_sync_of(p);
+  out->xy_bulk = p->l2 ? p->xy_bulk + 1 : 0;
   return ASG_OK;
 }
 
@@ -1693,10 +1696,12 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
     return fail(ASG_ERR_ARG, "cluster caps %d, %d outside 0..%d", t->xy_clusters,
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
   if (t->xy_sync < 0 || t->xy_sync > 2) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..2", t->xy_sync);
+  if (t->xy_bulk < 0 || t->xy_bulk > 3) return fail(ASG_ERR_ARG, "xy_bulk %d outside 0..3", t->xy_bulk);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
   p->xy_sync = t->xy_sync;
+  p->xy_bulk = t->xy_bulk == 0 ? 1 : t->xy_bulk - 1;
   p->gen++;
   return ASG_OK;
 }
@@ -1773,6 +1778,26 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
       }
     }
     p->xy_clusters = best_n;
+  }
+  if (p->l2 && status == ASG_OK) {
+    // HBM row loads of the plane kernels: cp.async, or bulk copies in the
+    // diffraction kernel, or in both (diffraction and closing passes together)
+    const bool closing = p->cfg.freq_weighted || p->cfg.super_absorbing;
+    double best = 1e300;
+    int best_b = 1;
+    for (int b : {0, 1, 2}) {
+      p->xy_bulk = b;
+      double ms = 0.0, ms_c = 0.0;
+      status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);
+      if (status != ASG_OK) break;
+      if (closing)
+        ms_c = p->launches[ASG_K_XY_C] > 0 ? p->kms[ASG_K_XY_C] / p->launches[ASG_K_XY_C] : 0.0;
+      if (ms + ms_c < best) {
+        best = ms + ms_c;
+        best_b = b;
+      }
+    }
+    p->xy_bulk = best_b;
   }
   // the closing-stage kernel runs when the step has a boundary epilogue
   if (p->l2 && (p->cfg.freq_weighted || p->cfg.super_absorbing) && status == ASG_OK) {

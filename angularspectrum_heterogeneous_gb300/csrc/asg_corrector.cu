@@ -1137,7 +1137,10 @@ __global__ void __launch_bounds__(256) k_flux_gate(GateParams p) {
       nsub = (q > (float)p.max_sub) ? p.max_sub : (int)q;
     }
   }
-  const bool learned = nsub >= p.min_sub && steep <= p.shock_ratio * s && s > 1e-30f;
+  // the coarse SSP-RK2 KT step is only a meaningful start below CFL 0.5 (its
+  // stability bound); columns above take the plain sub-cycled step
+  const bool learned = nsub >= p.min_sub && steep <= p.shock_ratio * s && s > 1e-30f &&
+                       p.ndt * s * p.dz <= 0.5f;
   if (!learned && lane == 0 && p.cfl_target > 0.f) {
     // a fallback column capped at max_sub sub-cycles runs above its CFL target
     const float q = ceilf(p.ndt * s * p.dz / p.cfl_target);

@@ -102,6 +102,8 @@ struct XYParams {
   unsigned grp_skew;       // added to every barrier target (test hook: 0 in normal runs)
   float2* spec_tmp;        // [planes][X][Y] work spectrum of the large generic planes
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
+  int bulk_rows;           // L2-exchange kernels' HBM row loads: 0 cp.async, 1 bulk copies in
+                           // the diffraction kernel, 2 bulk copies in both kernels
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);

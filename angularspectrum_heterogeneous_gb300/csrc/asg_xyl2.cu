@@ -40,6 +40,88 @@ ASG_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "
 
 ASG_DEV bool is_dc_or_nyq_l2(int f, int nT) { return f == 0 || 2 * f == nT; }
 
+// ---- bulk (TMA) row loads --------------------------------------------------
+// The spectrum rows a warp transforms in stage 1 come from HBM as 1-D bulk
+// async copies (cp.async.bulk, the copy engine moves them; one instruction per
+// segment instead of one 16-byte cp.async per lane), one segment per N2 slots
+// (the padded row layout puts two slots of padding after every N2), completing
+// on the warp's own mbarrier.  Segments are N2 * 8 bytes (128, 192 or 256),
+// row strides and segment offsets in shared memory multiples of 16 bytes, and
+// the sources are rows of a cudaMalloc'd spectrum: every bulk-copy alignment
+// rule holds for the supported planes (Y in 128..512).  The rows were written
+// by an earlier kernel, so no proxy fence is needed on the global side.
+ASG_DEV unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+ASG_DEV void mbar_init(uint64_t* mb, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb)), "r"(count) : "memory");
+}
+ASG_DEV void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+ASG_DEV void mbar_expect_tx(uint64_t* mb, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)),
+               "r"(bytes) : "memory");
+}
+ASG_DEV bool mbar_try_wait(uint64_t* mb, unsigned parity) {
+  unsigned ok = 0;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok) : "r"(smem_u32(mb)), "r"(parity) : "memory");
+  return ok != 0;
+}
+ASG_DEV void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* mb) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(mb)) : "memory");
+}
+// orders this thread's earlier generic accesses to shared memory before later
+// async-proxy (bulk copy) writes to it
+ASG_DEV void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// A warp's bulk loads of RPW rows: every lane fences its generic accesses to
+// the rows, lane 0 arms the mbarrier with the byte count, the lanes issue the
+// segments.  rows_src(j) gives the global start of row j, rows_dst(j) its
+// shared-memory row.
+template <class PY, int RPW, class Src, class Dst>
+ASG_DEV void warp_bulk_rows(uint64_t* mb, int lane, Src rows_src, Dst rows_dst) {
+  constexpr int SEG = PY::N2;              // slots per segment
+  constexpr int NSEG = PY::N / SEG;         // segments per row
+  constexpr unsigned BYTES = SEG * sizeof(float2);
+  static_assert(BYTES % 16 == 0 && ((SEG + 2) * sizeof(float2)) % 16 == 0 &&
+                    (PY::PADDED * sizeof(float2)) % 16 == 0,
+                "bulk-copy alignment");
+  fence_proxy_async_smem();
+  __syncwarp();
+  if (lane == 0) mbar_expect_tx(mb, RPW * NSEG * BYTES);
+  __syncwarp();
+  for (int i = lane; i < RPW * NSEG; i += 32) {
+    const int j = i / NSEG, sg = i - j * NSEG;
+    bulk_g2s(rows_dst(j) + sg * (SEG + 2), rows_src(j) + sg * SEG, BYTES, mb);
+  }
+}
+
+// Bounded wait for the warp's mbarrier phase `parity`: gives up after one
+// second (or as soon as the status word is set), records ASG_ERR_TIMEOUT if
+// nothing else was recorded, and returns false.
+ASG_DEV bool mbar_wait_bounded(uint64_t* mb, unsigned parity, unsigned* status) {
+  unsigned long long t0 = 0;
+  for (unsigned it = 0;; ++it) {
+    if (mbar_try_wait(mb, parity)) return true;
+    if ((it & 63) == 63) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > 1000000000ull) {
+        atomicCAS(status, 0u, (unsigned)(-ASG_ERR_TIMEOUT));
+        return false;
+      }
+    }
+  }
+}
+
 ASG_DEV bool l2_should_skip(const XYParams& p) {
   if (*((volatile const unsigned*)p.status) != 0u) return true;
   if (p.check_stability) {
@@ -127,6 +209,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   const int cid = blockIdx.x / G, ncl = gridDim.x / G;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   __shared__ int sync_ok;
+  __shared__ uint64_t row_mbar[NW];  // bulk row loads of each warp
+  __shared__ int rows_failed;
   unsigned arrivals = 0;
   // the group barrier: cluster barrier, or the counter barrier of a cooperative launch
   auto gsync = [&]() -> bool {
@@ -141,6 +225,14 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   const int nsub = p.nsub;
   const int nq = p.nplanes * nsub;
   if (l2_should_skip(p)) return;
+  if (lane == 0) {
+    mbar_init(&row_mbar[warp], 1);
+    mbar_init_fence();
+  }
+  if (tid == 0) rows_failed = 0;
+  __syncthreads();
+  unsigned row_phase = 0;
+  bool row_pending = false;
 
   for (int i = tid; i < Y; i += NT) {
     tw_y[i] = p.twY[i];
@@ -157,10 +249,23 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     const int plane = q / nsub, h = q - (q / nsub) * nsub;
     return p.spec + ((size_t)plane * p.X + (size_t)h * Xs) * Y;
   };
-  auto prefetch_row = [&](int q, int r) {
-    const float2* g = sub_base(q) + (size_t)(rank * R + r) * Y;
-    float2* d = buf + r * RS;
-    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
+  // loads of my warp's rows of (sub-)plane q: bulk copies, or 16-byte cp.async
+  const bool bulk = p.bulk_rows != 0;
+  auto prefetch_rows = [&](int q) {
+    const float2* g0 = sub_base(q) + (size_t)(rank * R + warp) * Y;
+    float2* d0 = buf + warp * RS;
+    if (bulk) {
+      warp_bulk_rows<PY, RPW>(
+          &row_mbar[warp], lane, [&](int j) { return g0 + (size_t)NW * j * Y; },
+          [&](int j) { return d0 + NW * j * RS; });
+      row_pending = true;
+    } else {
+#pragma unroll
+      for (int j = 0; j < RPW; ++j)
+        for (int s2 = lane; s2 < Y / 2; s2 += 32)
+          cp_async16(d0 + NW * j * RS + PY::pos(2 * s2), g0 + (size_t)NW * j * Y + 2 * s2);
+      cp_async_commit();
+    }
   };
   int issued = -1;
 
@@ -175,13 +280,15 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     // only its own rows, and the cluster barriers order stage 2's accesses to
     // all rows after every CTA's stage 3 of the previous plane
     float2* S = scratch0;
-    if (issued != q) {
-#pragma unroll
-      for (int j = 0; j < RPW; ++j) prefetch_row(q, warp + NW * j);
-      cp_async_commit();
+    if (issued != q) prefetch_rows(q);
+    if (row_pending) {
+      if (!mbar_wait_bounded(&row_mbar[warp], row_phase, p.status)) rows_failed = 1;
+      row_phase ^= 1u;
+      row_pending = false;
     }
     cp_async_wait_all();
     __syncthreads();
+    if (rows_failed) break;
 
     // ---- 1. forward y FFT on my rows (warp w: rows w + NW j, both rows'
     //      tasks share the warp's lanes), rows -> scratch (slot order) ----
@@ -344,15 +451,13 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     }
     __syncwarp();
     if (pref) {
-#pragma unroll
-      for (int j = 0; j < RPW; ++j) prefetch_row(qn, warp + NW * j);
-    }
-    if (pref) {
-      cp_async_commit();
+      prefetch_rows(qn);
       issued = qn;
     }
   }
   cp_async_wait_all();
+  // no bulk copy may still be landing in shared memory when the block exits
+  if (row_pending) mbar_wait_bounded(&row_mbar[warp], row_phase, p.status);
 }
 
 // ---------------------------------------------------------------------------
@@ -417,6 +522,14 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (*((volatile const unsigned*)p.status) != 0u) return;
   __shared__ int sync_ok;
+  __shared__ uint64_t row_mbar[NW];  // bulk row loads of each warp
+  if (lane == 0) {
+    mbar_init(&row_mbar[warp], 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  unsigned row_phase = 0;
+  bool row_pending = false;
   unsigned arrivals = 0;
   auto gsync = [&]() -> bool {
     if (coop) {
@@ -442,10 +555,24 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
   const bool fw = (p.epi & EPI_FREQW) != 0, sa = (p.epi & EPI_SUPERABS) != 0;
   const float st = p.sa_strength;
 
-  auto prefetch_row = [&](int plane, int h, int r) {
-    const float2* g = p.spec + ((size_t)plane * X + (size_t)h * Xs + rank * R + r) * Y;
-    float2* d = buf + r * RS;
-    for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(d + PY::pos(2 * s2), g + 2 * s2);
+  // loads of my warp's rows of half-plane h of `plane`: bulk copies (bulk_rows
+  // 2), or 16-byte cp.async
+  const bool bulk = p.bulk_rows >= 2;
+  auto prefetch_rows = [&](int plane, int h) {
+    const float2* g0 = p.spec + ((size_t)plane * X + (size_t)h * Xs + rank * R + warp) * Y;
+    float2* d0 = buf + warp * RS;
+    if (bulk) {
+      warp_bulk_rows<PY, RPW>(
+          &row_mbar[warp], lane, [&](int j) { return g0 + (size_t)NW * j * Y; },
+          [&](int j) { return d0 + NW * j * RS; });
+      row_pending = true;
+    } else {
+#pragma unroll
+      for (int j = 0; j < RPW; ++j)
+        for (int s2 = lane; s2 < Y / 2; s2 += 32)
+          cp_async16(d0 + NW * j * RS + PY::pos(2 * s2), g0 + (size_t)NW * j * Y + 2 * s2);
+      cp_async_commit();
+    }
   };
   int issued = -1;
 
@@ -463,10 +590,12 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
     //      loads of its rows of b as soon as its rows of a are stored ----
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
-      if (issued != plane * 2 + h) {
-#pragma unroll
-        for (int j = 0; j < RPW; ++j) prefetch_row(plane, h, warp + NW * j);
-        cp_async_commit();
+      if (issued != plane * 2 + h) prefetch_rows(plane, h);
+      if (row_pending) {
+        // on a timeout the status word is set and the run ends with it
+        mbar_wait_bounded(&row_mbar[warp], row_phase, p.status);
+        row_phase ^= 1u;
+        row_pending = false;
       }
       cp_async_wait_all();
       __syncwarp();
@@ -693,13 +822,13 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
     }
     // rows of a of my next plane, while the other warps finish
     if (plane + ncl < p.nplanes) {
-#pragma unroll
-      for (int j = 0; j < RPW; ++j) prefetch_row(plane + ncl, 0, warp + NW * j);
-      cp_async_commit();
+      prefetch_rows(plane + ncl, 0);
       issued = (plane + ncl) * 2;
     }
   }
   cp_async_wait_all();
+  // no bulk copy may still be landing in shared memory when the block exits
+  if (row_pending) mbar_wait_bounded(&row_mbar[warp], row_phase, p.status);
 }
 
 // ---------------------------------------------------------------------------

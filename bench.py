@@ -477,17 +477,19 @@ NET_FLOP_PER_SAMPLE = 2 * 5 * (1 * 64 + 64 * 64 + 64 * 64 + 64 * 1)  # 83,200
 
 def learned_params(steps):
     """The workload's medium and grid steps, KT, no boundary extras; 0.5 mm
-    march steps with the KT step sub-cycled per column at CFL 0.01 (the
-    stability threshold raised accordingly: every sub-step stays at CFL 0.01)."""
+    march steps with the KT step sub-cycled per column at CFL 0.01.  The
+    reference's stability threshold guards its single KT step per march step;
+    here every sub-step stays at CFL 0.01, so the threshold is lifted."""
     from angularspectrum_heterogeneous_gb300 import SolverParams
     return SolverParams(dX=1.5e-4, dY=1.5e-4, dT=1e-8, c0=1540.0, rho0=1000.0, beta=3.5,
                         alpha0=0.5, attenPow=1.0, f0=2e6, propDist=steps * LEARN_DZ,
-                        dZmin=LEARN_DZ, fluxScheme="kt", stabilityThreshold=2.0)
+                        dZmin=LEARN_DZ, fluxScheme="kt", stabilityThreshold=1e6)
 
 
 def learned_training_pool(n_fields=8, snapshots=4, per_snapshot=65536, seed=1):
-    """Columns of seeded random focused fields (peak 0.5-3 MPa, 1-3 MHz, on the
-    workload's 512x512x1024 grid) taken at `snapshots` depths while the plain
+    """Columns of seeded random focused fields (peak 0.5-3 MPa, 1-3 MHz, focus
+    40-80 mm, on the workload's 512x512x1024 grid) taken at `snapshots` depths
+    while the plain
     GPU KT solver marches them (0.5 mm steps, per-column sub-cycling at CFL
     0.01): n_fields * snapshots * per_snapshot device columns."""
     import torch
@@ -497,7 +499,8 @@ def learned_training_pool(n_fields=8, snapshots=4, per_snapshot=65536, seed=1):
     g = torch.Generator(device="cuda").manual_seed(seed)
     out = []
     for _ in range(n_fields):
-        u0, f0 = CR.random_focused_field((NX, NY, NT), rng, dX=1.5e-4, dT=1e-8)
+        u0, f0 = CR.random_focused_field((NX, NY, NT), rng, dX=1.5e-4, dT=1e-8,
+                                         focus_range=(40e-3, 80e-3))
         prm = learned_params(LEARN_STEPS)
         prm.f0 = f0
         takes = set(int(k) for k in np.linspace(LEARN_STEPS // 6, LEARN_STEPS - 1, snapshots))
@@ -559,7 +562,12 @@ def run_learned_arm(args):
 
     ms_plain, plain, _, clk, _ = march(LEARN_CFL, False)
     ms_learned, learned, (nl, ncs), _, _ = march(LEARN_CFL, True)
-    ms_coarse, coarse, _, _, _ = march(0.0, False)
+    from angularspectrum_heterogeneous_gb300 import ASGError
+    try:  # one KT step per column: above CFL 0.5 near the focus it may not stay finite
+        ms_coarse, coarse, _, _, _ = march(0.0, False)
+        coarse_note = None
+    except ASGError as e:
+        ms_coarse, coarse, coarse_note = float("nan"), None, str(e)[:200]
     # the network alone: forward of one step's learned columns
     xr = torch.randn(max(nl // LEARN_STEPS, 1), NT, device="cuda")
     net.forward(xr)
@@ -581,6 +589,8 @@ def run_learned_arm(args):
     kf = int(np.argmax(plain[2][cx, cy, :]))  # step of peak on-axis ppp
     errs = {}
     for name, out in (("learned", learned), ("coarse", coarse)):
+        if out is None:
+            continue
         for i, k in ((1, "pnp"), (2, "ppp"), (3, "pI")):
             errs[f"{name}_{k}"] = rel(out[i], plain[i])
             errs[f"{name}_{k}_focal_plane"] = rel(out[i][:, :, kf], plain[i][:, :, kf])
@@ -605,8 +615,9 @@ def run_learned_arm(args):
                        "final_loss": float(np.mean(hist[-20:])),
                        "learned_column_steps": int(nl), "column_steps": int(ncs)},
             "plain_kt_march": {"value": vs / (ms_plain / 1e3), "ms_per_step": ms_plain / LEARN_STEPS},
-            "coarse_kt_march": {"value": vs / (ms_coarse / 1e3),
-                                "ms_per_step": ms_coarse / LEARN_STEPS},
+            "coarse_kt_march": ({"value": vs / (ms_coarse / 1e3),
+                                 "ms_per_step": ms_coarse / LEARN_STEPS} if coarse is not None
+                                else {"failed": coarse_note}),
             "speedup_vs_plain": ms_plain / ms_learned,
             "rel_l2_vs_plain_gpu_march": errs, "focal_step": kf,
             "network": {"ms": ms_net, "tflops": net_tf,

@@ -204,6 +204,10 @@ typedef struct {
                       * barrier in a cooperative launch, which is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
                       * beside other heavy work on the same GPU) */
+  int xy_bulk;       /* HBM row loads of those kernels: 1 16-byte cp.async per lane, 2 bulk
+                      * async copies (cp.async.bulk, one per row segment, mbarrier
+                      * completion) in the diffraction kernel, 3 bulk copies in the
+                      * closing-stage kernel too; 0 = default (2) */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of
@@ -295,7 +299,9 @@ int asg_net_set_output_scale(asg_net* net, float gamma);
 /* Learned KT step on device columns (in -> out, ncols x nT floats, nT a
  * multiple of 128 up to 1024; in != out).  Per column: s = max|u|, the plain
  * KT sub-cycle count n_sub at cfl_target, and the steepness max|u[t+1]-u[t]|.
- * When n_sub >= min_subcycles and the steepness is at most shock_ratio * s,
+ * When n_sub >= min_subcycles, the steepness is at most shock_ratio * s and the
+ * column's CFL number n_coef/dt * s * dz is at most 0.5 (the stability bound of
+ * the coarse step),
  * one coarse KT step of the full dz plus the scaled correction above; otherwise
  * the plain sub-cycled KT step (the fallback).  Synchronous; *n_learned
  * receives the number of corrected columns. */
