@@ -515,7 +515,7 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
       }
     CKS(dalloc(&p->l2_cls_x, 2 * Xs));
     CKS(h2d(p->l2_cls_x, cl.data(), 2 * Xs, p->st));
-    CKS(dalloc(&p->grp_cnt, L2_MAX_CLUSTERS));
+    CKS(dalloc(&p->grp_cnt, 2 * L2_MAX_CLUSTERS));
   }
   CKS(dalloc(&p->real, (size_t)p->ncols * T));
   std::vector<float2> w;
@@ -912,7 +912,8 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.l2_cls_x = p->l2_cls_x;
   x.l2_max_clusters = (p->xy_clusters > 0 && p->xy_clusters < L2_MAX_CLUSTERS)
                           ? p->xy_clusters : L2_MAX_CLUSTERS;
-  x.coop = xy_sync_of(p) == 2 ? 1 : 0;
+  x.coop = xy_sync_of(p) >= 2 ? 1 : 0;
+  x.pipe = xy_sync_of(p) == 3 ? 1 : 0;
   x.bulk_rows = p->xy_bulk;
   x.grp_cnt = p->grp_cnt;
   x.grp_skew = p->barrier_skew;
@@ -1695,7 +1696,7 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
       t->xy_clusters_closing < 0 || t->xy_clusters_closing > L2_MAX_CLUSTERS)
     return fail(ASG_ERR_ARG, "cluster caps %d, %d outside 0..%d", t->xy_clusters,
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
-  if (t->xy_sync < 0 || t->xy_sync > 2) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..2", t->xy_sync);
+  if (t->xy_sync < 0 || t->xy_sync > 3) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..3", t->xy_sync);
   if (t->xy_bulk < 0 || t->xy_bulk > 3) return fail(ASG_ERR_ARG, "xy_bulk %d outside 0..3", t->xy_bulk);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
@@ -1748,7 +1749,7 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
     const bool closing = p->cfg.freq_weighted || p->cfg.super_absorbing;
     double best = 1e300;
     int best_s = 0;
-    for (int sy : {1, 2}) {
+    for (int sy : {1, 2, 3}) {
       p->xy_sync = sy;
       double ms = 0.0, ms_c = 0.0;
       status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);

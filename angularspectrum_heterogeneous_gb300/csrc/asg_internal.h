@@ -98,7 +98,9 @@ struct XYParams {
   int l2_max_clusters;     // clusters the scratch was sized for
   int coop;                // 1: CTA groups of a cooperative launch synchronised by
                            //    counters in grp_cnt instead of thread-block clusters
-  unsigned* grp_cnt;       // [l2_max_clusters] arrival counters (zeroed by the launcher)
+  unsigned* grp_cnt;       // [2][l2_max_clusters] arrival counters (zeroed by the launcher;
+                           //    the second set is used by the pipelined flow)
+  int pipe;                // 1 (with coop): split-phase barriers over two scratch halves
   unsigned grp_skew;       // added to every barrier target (test hook: 0 in normal runs)
   float2* spec_tmp;        // [planes][X][Y] work spectrum of the large generic planes
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   };
   // loads of my warp's rows of (sub-)plane q: bulk copies, or 16-byte cp.async
   const bool bulk = p.bulk_rows != 0;
-  auto prefetch_rows = [&](int q) {
+  auto load_rows = [&](int q) {
     const float2* g0 = sub_base(q) + (size_t)(rank * R + warp) * Y;
     float2* d0 = buf + warp * RS;
     if (bulk) {
@@ -267,20 +267,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       cp_async_commit();
     }
   };
-  int issued = -1;
-
-  for (int q = cid; q < nq; q += ncl) {
-    const int plane = q / nsub, h = q - (q / nsub) * nsub;
-    if (zero_plane(q)) {
-      float4* g4 = reinterpret_cast<float4*>(sub_base(q) + (size_t)rank * R * Y);
-      for (int i = tid; i < R * Y / 2; i += NT) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-      continue;
-    }
-    // one scratch half-plane per cluster: in stages 1 and 3 each CTA touches
-    // only its own rows, and the cluster barriers order stage 2's accesses to
-    // all rows after every CTA's stage 3 of the previous plane
-    float2* S = scratch0;
-    if (issued != q) prefetch_rows(q);
+  // waits for my warp's rows, then for the whole block; false after a timeout
+  auto wait_rows = [&]() -> bool {
     if (row_pending) {
       if (!mbar_wait_bounded(&row_mbar[warp], row_phase, p.status)) rows_failed = 1;
       row_phase ^= 1u;
@@ -288,10 +276,16 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
     }
     cp_async_wait_all();
     __syncthreads();
-    if (rows_failed) break;
+    return rows_failed == 0;
+  };
+  auto zero_rows = [&](int q) {
+    float4* g4 = reinterpret_cast<float4*>(sub_base(q) + (size_t)rank * R * Y);
+    for (int i = tid; i < R * Y / 2; i += NT) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  };
 
-    // ---- 1. forward y FFT on my rows (warp w: rows w + NW j, both rows'
-    //      tasks share the warp's lanes), rows -> scratch (slot order) ----
+  // ---- 1. forward y FFT on my rows (warp w: rows w + NW j, both rows'
+  //      tasks share the warp's lanes), rows -> scratch S (slot order) ----
+  auto stage1 = [&](float2* S) {
     for (int i = lane; i < RPW * PY::N2; i += 32) {
       const int j = i / PY::N2, b = i - j * PY::N2;
       stepA_fwd_smem<PY, false>(buf + (warp + NW * j) * RS, b, tw_y);
@@ -310,113 +304,111 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int s2 = lane; s2 < Y / 2; s2 += 32)
         dst[s2] = *reinterpret_cast<const float4*>(row + PY::pos(2 * s2));
     }
-    // the barrier (release / acquire) orders these global writes before the
-    // other CTAs' reads of the scratch
-    if (!gsync()) break;
+  };
 
-    // ---- 2. columns [rank*Yc, +Yc) of all Xs rows: x FFT, multiplier, inverse ----
-    {
-      const int c0 = rank * Yc;
-      // tile[x][c], row stride TS
-      for (int i = tid; i < Xs * Yc / 2; i += NT) {
-        const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
-        cp_async16(buf + x * TS + c2, S + (size_t)x * Y + c0 + c2);
-      }
-      cp_async_commit();
-      cp_async_wait_all();
-      __syncthreads();
-      // step A (forward): task (b, c), elements x = b + N2x*a
-      for (int it = tid; it < PX::N2 * Yc; it += NT) {
-        const int b = it / Yc, c = it - b * Yc;
-        float2 v[PX::N1];
+  // ---- 2. columns [rank*Yc, +Yc) of all Xs rows: x FFT, multiplier (or the
+  //      power sums), inverse; ends with the block's tile writes to S issued ----
+  auto stage2 = [&](int q, float2* S) {
+    const int plane = q / nsub, h = q - (q / nsub) * nsub;
+    const int c0 = rank * Yc;
+    // tile[x][c], row stride TS
+    for (int i = tid; i < Xs * Yc / 2; i += NT) {
+      const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
+      cp_async16(buf + x * TS + c2, S + (size_t)x * Y + c0 + c2);
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    // step A (forward): task (b, c), elements x = b + N2x*a
+    for (int it = tid; it < PX::N2 * Yc; it += NT) {
+      const int b = it / Yc, c = it - b * Yc;
+      float2 v[PX::N1];
 #pragma unroll
-        for (int a = 0; a < PX::N1; ++a) v[a] = buf[(b + PX::N2 * a) * TS + c];
-        dft<PX::N1, false>(v);
-        buf[b * TS + c] = v[0];
+      for (int a = 0; a < PX::N1; ++a) v[a] = buf[(b + PX::N2 * a) * TS + c];
+      dft<PX::N1, false>(v);
+      buf[b * TS + c] = v[0];
 #pragma unroll
-        for (int ka = 1; ka < PX::N1; ++ka) buf[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x[b * ka]);
-      }
-      __syncthreads();
-      float psum = 0.f, pden = 0.f;
-      // step B forward, multiplier, step B inverse: task (ka, c), slots kb + N2x*ka
-      for (int it = tid; it < PX::N1 * Yc; it += NT) {
-        const int ka = it / Yc, c = it - ka * Yc;
-        float2 v[PX::N2];
+      for (int ka = 1; ka < PX::N1; ++ka) buf[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x[b * ka]);
+    }
+    __syncthreads();
+    float psum = 0.f, pden = 0.f;
+    // step B forward, multiplier, step B inverse: task (ka, c), slots kb + N2x*ka
+    for (int it = tid; it < PX::N1 * Yc; it += NT) {
+      const int ka = it / Yc, c = it - ka * Yc;
+      float2 v[PX::N2];
 #pragma unroll
-        for (int b = 0; b < PX::N2; ++b) v[b] = buf[(b + PX::N2 * ka) * TS + c];
-        dft<PX::N2, false>(v);
-        const int cy = clsy[c0 + c];
-        const int* cxh = clsx + h * Xs;
-        if (p.power_only) {
-          const float* ot = p.obl_table + (size_t)plane * p.ncx * p.ncy + cy;
-#pragma unroll
-          for (int kb = 0; kb < PX::N2; ++kb) {
-            const float o = ot[(size_t)cxh[kb + PX::N2 * ka] * p.ncy];
-            const float P = v[kb].x * v[kb].x + v[kb].y * v[kb].y;
-            psum = fmaf(P, o, psum);
-            pden += (o > 0.f) ? P : 0.f;
-          }
-          continue;
-        }
-        if (p.table != nullptr) {
-          const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + cy;
-#pragma unroll
-          for (int kb = 0; kb < PX::N2; ++kb)
-            v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
-        } else {
-          const float nrm = 1.0f / ((float)Xs * (float)Y);
-#pragma unroll
-          for (int kb = 0; kb < PX::N2; ++kb) v[kb] = cscale(v[kb], nrm);
-        }
-        dft<PX::N2, true>(v);
-#pragma unroll
-        for (int b = 0; b < PX::N2; ++b) buf[(b + PX::N2 * ka) * TS + c] = v[b];
-      }
+      for (int b = 0; b < PX::N2; ++b) v[b] = buf[(b + PX::N2 * ka) * TS + c];
+      dft<PX::N2, false>(v);
+      const int cy = clsy[c0 + c];
+      const int* cxh = clsx + h * Xs;
       if (p.power_only) {
-        psum = warp_sum(psum);
-        pden = warp_sum(pden);
-        if (lane == 0) {
-          red[0][warp] = psum;
-          red[1][warp] = pden;
+        const float* ot = p.obl_table + (size_t)plane * p.ncx * p.ncy + cy;
+#pragma unroll
+        for (int kb = 0; kb < PX::N2; ++kb) {
+          const float o = ot[(size_t)cxh[kb + PX::N2 * ka] * p.ncy];
+          const float P = v[kb].x * v[kb].x + v[kb].y * v[kb].y;
+          psum = fmaf(P, o, psum);
+          pden += (o > 0.f) ? P : 0.f;
         }
-        __syncthreads();
-        if (tid == 0) {
-          double a = 0.0, b = 0.0;
-          for (int w = 0; w < NW; ++w) {
-            a += (double)red[0][w];
-            b += (double)red[1][w];
-          }
-          atomicAdd(p.power_acc, a);
-          atomicAdd(p.power_acc + 1, b);
-        }
-        // no CTA reuses the scratch before every CTA has read it
-        if (!gsync()) break;
         continue;
       }
-      __syncthreads();
-      // step A inverse: task (b, c)
-      for (int it = tid; it < PX::N2 * Yc; it += NT) {
-        const int b = it / Yc, c = it - b * Yc;
-        float2 v[PX::N1];
-        v[0] = buf[b * TS + c];
+      if (p.table != nullptr) {
+        const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + cy;
 #pragma unroll
-        for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(buf[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
-        dft<PX::N1, true>(v);
+        for (int kb = 0; kb < PX::N2; ++kb)
+          v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
+      } else {
+        const float nrm = 1.0f / ((float)Xs * (float)Y);
 #pragma unroll
-        for (int a = 0; a < PX::N1; ++a) buf[(b + PX::N2 * a) * TS + c] = v[a];
+        for (int kb = 0; kb < PX::N2; ++kb) v[kb] = cscale(v[kb], nrm);
       }
-      __syncthreads();
-      for (int i = tid; i < Xs * Yc / 2; i += NT) {
-        const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
-        *reinterpret_cast<float4*>(S + (size_t)x * Y + c0 + c2) =
-            *reinterpret_cast<const float4*>(buf + x * TS + c2);
-      }
+      dft<PX::N2, true>(v);
+#pragma unroll
+      for (int b = 0; b < PX::N2; ++b) buf[(b + PX::N2 * ka) * TS + c] = v[b];
     }
-    if (!gsync()) break;
+    if (p.power_only) {
+      psum = warp_sum(psum);
+      pden = warp_sum(pden);
+      if (lane == 0) {
+        red[0][warp] = psum;
+        red[1][warp] = pden;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < NW; ++w) {
+          a += (double)red[0][w];
+          b += (double)red[1][w];
+        }
+        atomicAdd(p.power_acc, a);
+        atomicAdd(p.power_acc + 1, b);
+      }
+      return;
+    }
+    __syncthreads();
+    // step A inverse: task (b, c)
+    for (int it = tid; it < PX::N2 * Yc; it += NT) {
+      const int b = it / Yc, c = it - b * Yc;
+      float2 v[PX::N1];
+      v[0] = buf[b * TS + c];
+#pragma unroll
+      for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(buf[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
+      dft<PX::N1, true>(v);
+#pragma unroll
+      for (int a = 0; a < PX::N1; ++a) buf[(b + PX::N2 * a) * TS + c] = v[a];
+    }
+    __syncthreads();
+    for (int i = tid; i < Xs * Yc / 2; i += NT) {
+      const int x = i / (Yc / 2), c2 = 2 * (i - x * (Yc / 2));
+      *reinterpret_cast<float4*>(S + (size_t)x * Y + c0 + c2) =
+          *reinterpret_cast<const float4*>(buf + x * TS + c2);
+    }
+  };
 
-    // ---- 3. my rows back from the scratch, inverse y FFT, store ----
-    // (cp.async.cg reads L2: other CTAs wrote these rows; each warp copies and
-    // then transforms only its own rows)
+  // ---- 3. my rows back from the scratch (cp.async.cg reads L2: other CTAs
+  //      wrote these rows; each warp copies and then transforms only its own
+  //      rows), inverse y FFT, store ----
+  auto stage3 = [&](int q, float2* S) {
 #pragma unroll
     for (int j = 0; j < RPW; ++j) {
       const int r = warp + NW * j;
@@ -425,9 +417,6 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int s2 = lane; s2 < Y / 2; s2 += 32) cp_async16(row + PY::pos(2 * s2), srcr + 2 * s2);
     }
     cp_async_commit();
-    int qn = q + ncl;
-    while (qn < nq && zero_plane(qn)) qn += ncl;
-    const bool pref = qn < nq;
     cp_async_wait_all();
     __syncwarp();
     float2* gbase = sub_base(q) + (size_t)rank * R * Y;
@@ -450,9 +439,116 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       for (int a = 0; a < PY::N1; ++a) grow[b + PY::N2 * a] = v[a];
     }
     __syncwarp();
-    if (pref) {
-      prefetch_rows(qn);
-      issued = qn;
+  };
+  auto next_plane = [&](int q) {
+    q += ncl;
+    while (q < nq && zero_plane(q)) q += ncl;
+    return q;
+  };
+
+  if (coop && p.pipe && !p.power_only) {
+    // ---- pipelined flow: split-phase counter barriers over two scratch halves.
+    // Per plane i: arrive at barrier 1 after stage 1, wait before stage 2;
+    // arrive at barrier 2 after stage 2, wait before stage 3.  Between the
+    // arrival at barrier 2 of plane i and its wait, the block runs stage 1 of
+    // plane i+1 (into the other scratch half); between the arrival at barrier
+    // 1 of plane i+1 and its wait, stage 3 of plane i.  Two counters per group
+    // (arrivals at the two barriers) with targets G (i + 1): arriving at a
+    // barrier for plane i+1 needs the wait of plane i at the same barrier,
+    // so a count can only reach its target through the arrivals it waits for.
+    // Scratch half i&1: stage 1 of plane i+2 rewrites my rows of it only after
+    // my stage 3 of plane i (program order), and every block's stage 2 of
+    // plane i+2 only after barrier 1 of plane i+2, which every block reaches
+    // after its own stage 3 of plane i.
+    unsigned* c1 = p.grp_cnt + cid;
+    unsigned* c2 = p.grp_cnt + p.l2_max_clusters + cid;
+    auto arrive = [&](unsigned* cnt) {
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        atomicAdd(cnt, 1u);
+      }
+    };
+    auto wait = [&](unsigned* cnt, unsigned target) -> bool {
+      if (tid == 0) {
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        while (*((volatile unsigned*)cnt) < target) {
+          if (*((volatile unsigned*)p.status) != 0u) {
+            ok = 0;
+            break;
+          }
+          if (global_ns() - t0 > 1000000000ull) {
+            atomicCAS(p.status, 0u, (unsigned)(-ASG_ERR_TIMEOUT));
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+        __threadfence();
+        sync_ok = ok;
+      }
+      __syncthreads();
+      return sync_ok != 0;
+    };
+    for (int q = cid; q < nq; q += ncl)
+      if (zero_plane(q)) zero_rows(q);
+    int q = cid;
+    while (q < nq && zero_plane(q)) q += ncl;
+    if (q < nq) {
+      load_rows(q);
+      if (wait_rows()) {
+        stage1(scratch0);
+        arrive(c1);
+      } else {
+        q = nq;
+      }
+    }
+    for (unsigned i = 0; q < nq; ++i) {
+      float2* Sc = scratch0 + (size_t)(i & 1u) * Xs * Y;
+      float2* Sn = scratch0 + (size_t)((i + 1) & 1u) * Xs * Y;
+      if (!wait(c1, G * (i + 1) + p.grp_skew)) break;
+      stage2(q, Sc);
+      const int qn = next_plane(q);
+      __syncthreads();  // the tile is written out: the row buffer is free
+      if (qn < nq) load_rows(qn);
+      arrive(c2);
+      if (qn < nq) {
+        if (!wait_rows()) break;
+        stage1(Sn);
+        arrive(c1);
+      }
+      if (!wait(c2, G * (i + 1) + p.grp_skew)) break;
+      stage3(q, Sc);
+      q = qn;
+    }
+  } else {
+    int issued = -1;
+    for (int q = cid; q < nq; q += ncl) {
+      if (zero_plane(q)) {
+        zero_rows(q);
+        continue;
+      }
+      // one scratch half-plane per cluster: in stages 1 and 3 each CTA touches
+      // only its own rows, and the cluster barriers order stage 2's accesses to
+      // all rows after every CTA's stage 3 of the previous plane
+      float2* S = scratch0;
+      if (issued != q) load_rows(q);
+      if (!wait_rows()) break;
+      stage1(S);
+      // the barrier (release / acquire) orders these global writes before the
+      // other CTAs' reads of the scratch
+      if (!gsync()) break;
+      stage2(q, S);
+      // power sums: no CTA reuses the scratch before every CTA has read it
+      if (!gsync()) break;
+      if (p.power_only) continue;
+      stage3(q, S);
+      const int qn = next_plane(q);
+      if (qn < nq) {
+        load_rows(qn);
+        issued = qn;
+      }
     }
   }
   cp_async_wait_all();
@@ -875,7 +971,9 @@ static int launch_groups(K kern, const XYParams& p, cudaLaunchConfig_t cfg, int 
     if (p.grp_cnt == nullptr) return ASG_ERR_ARG;
     // every CTA of the grid is resident, so the counter barriers of a group
     // always complete
-    if (cudaMemsetAsync(p.grp_cnt, 0, (size_t)ng * sizeof(unsigned), st) != cudaSuccess)
+    if (cudaMemsetAsync(p.grp_cnt, 0, (size_t)ng * sizeof(unsigned), st) != cudaSuccess ||
+        cudaMemsetAsync(p.grp_cnt + p.l2_max_clusters, 0, (size_t)ng * sizeof(unsigned), st) !=
+            cudaSuccess)
       return ASG_ERR_CUDA;
     coop[0].id = cudaLaunchAttributeCooperative;
     coop[0].val.cooperative = 1;

@@ -201,7 +201,10 @@ typedef struct {
   int xy_clusters;   /* cap on resident CTA groups (clusters) of the L2-exchange plane kernel: 0..64 */
   int xy_clusters_closing; /* the same for the closing-stage kernel (fused epilogue): 0..64 */
   int xy_sync;       /* group barrier of those kernels: 1 thread-block cluster, 2 counter
-                      * barrier in a cooperative launch, which is sized to fill the GPU
+                      * barrier in a cooperative launch, 3 the same with split-phase
+                      * barriers over two scratch halves in the diffraction kernel (the
+                      * block runs the next plane's first stage, or this plane's last,
+                      * between arriving at a barrier and waiting on it); the launch is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
                       * beside other heavy work on the same GPU) */
   int xy_bulk;       /* HBM row loads of those kernels: 1 16-byte cp.async per lane, 2 bulk

@@ -41,7 +41,9 @@ def test_every_shape_gives_the_same_march(shape, flux):
                   dict(t_cols_flux=16, t_cols_plain=16, t_cols_stats=16, xy_clusters=3,
                        xy_clusters_closing=0, xy_sync=2, xy_bulk=3),
                   dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
-                       xy_clusters_closing=0, xy_sync=2)]
+                       xy_clusters_closing=0, xy_sync=2),
+                  dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=5,
+                       xy_clusters_closing=0, xy_sync=3, xy_bulk=2)]
         for tun in shapes:
             plan.set_tuning(tun)
             got = plan.get_tuning()
@@ -74,11 +76,12 @@ def test_unsupported_shape_is_rejected():
         plan.close()
 
 
-def test_group_barrier_wait_runs_out_and_the_plan_recovers():
-    """The counter barriers of the cooperative plane kernels are bounded: with
-    a target no group reaches, every wait gives up after a second, the run
-    ends with ASG_ERR_TIMEOUT, and the next run (normal targets) matches the
-    earlier one bit for bit."""
+@pytest.mark.parametrize("sync", [2, 3])
+def test_group_barrier_wait_runs_out_and_the_plan_recovers(sync):
+    """The counter barriers of the cooperative plane kernels (plain, and split
+    into arrive and wait) are bounded: with a target no group reaches, every
+    wait gives up after a second, the run ends with ASG_ERR_TIMEOUT, and the
+    next run (normal targets) matches the earlier one bit for bit."""
     from angularspectrum_heterogeneous_gb300 import Plan
     from angularspectrum_heterogeneous_gb300._lib import ASGError
     from angularspectrum_heterogeneous_gb300.solver import initial_step
@@ -89,8 +92,8 @@ def test_group_barrier_wait_runs_out_and_the_plan_recovers():
     try:
         plan.set_operators(0, dz)
         plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
-                             xy_clusters_closing=0, xy_sync=2))
-        assert plan.get_tuning()["xy_sync"] == 2
+                             xy_clusters_closing=0, xy_sync=sync))
+        assert plan.get_tuning()["xy_sync"] == sync
         ref = _run(plan, u0, dz, steps=2)
         _lib_check(plan, 1)
         with pytest.raises(ASGError) as e:
