@@ -209,6 +209,7 @@ struct asg_plan {
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
   int xy_bulk = 1;            // HBM row loads of the L2 plane kernels (XYParams::bulk_rows)
+  int t_prefetch = 0;         // column passes: L2 prefetch of a later tile (TParams::prefetch)
   int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
                               // 1 thread-block cluster, 2 counters in a cooperative launch
   int batch_refs = 0;         // batches holding the plan (they use cluster barriers)
@@ -933,6 +934,7 @@ static int run_t(asg_plan* p, const TParams& t, int kind = ASG_K_OTHER) {
   if (!p->tfast) return asg_launch_t(t, false, p->gp_t, p->st);
   TParams tt = t;
   tt.cols_per_block = p->t_cols[t_slot(t)];
+  tt.prefetch = p->t_prefetch;
   return asg_launch_t(tt, true, p->gp_t, p->st);
 }
 static int run_xy(asg_plan* p, const XYParams& x, int kind = ASG_K_OTHER) {
@@ -1679,6 +1681,7 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   out->xy_clusters_closing = p->l2 ? ncl : 0;
   out->xy_sync = xy_sync_of(p);
   out->xy_bulk = p->l2 ? p->xy_bulk + 1 : 0;
+  out->t_prefetch = p->tfast ? p->t_prefetch + 1 : 0;
   return ASG_OK;
 }
 
@@ -1698,11 +1701,14 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
   if (t->xy_sync < 0 || t->xy_sync > 3) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..3", t->xy_sync);
   if (t->xy_bulk < 0 || t->xy_bulk > 3) return fail(ASG_ERR_ARG, "xy_bulk %d outside 0..3", t->xy_bulk);
+  if (t->t_prefetch < 0 || t->t_prefetch > 2)
+    return fail(ASG_ERR_ARG, "t_prefetch %d outside 0..2", t->t_prefetch);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
   p->xy_sync = t->xy_sync;
   p->xy_bulk = t->xy_bulk == 0 ? 1 : t->xy_bulk - 1;
+  p->t_prefetch = t->t_prefetch == 0 ? 0 : t->t_prefetch - 1;
   p->gen++;
   return ASG_OK;
 }
@@ -1743,6 +1749,23 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
       }
       p->t_cols[i] = best_c;
     }
+    // L2 prefetch of later tiles: the three column passes together
+    double best = 1e300;
+    int best_f = 0;
+    for (int f : {0, 1}) {
+      if (status != ASG_OK) break;
+      p->t_prefetch = f;
+      double ms = 0.0;
+      status = trial(ASG_K_T_NONLIN, &ms);
+      if (status != ASG_OK) break;
+      for (int k : {ASG_K_T_MID, ASG_K_T_END})
+        if (p->launches[k] > 0) ms += p->kms[k] / p->launches[k];
+      if (ms < best) {
+        best = ms;
+        best_f = f;
+      }
+    }
+    p->t_prefetch = best_f;
   }
   if (p->l2 && status == ASG_OK && p->batch_refs == 0) {
     // group barrier: the plain diffraction pass and the closing pass together

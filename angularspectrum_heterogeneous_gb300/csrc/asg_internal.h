@@ -31,6 +31,9 @@ struct TParams {
   const float2* twM;     // W_M^k,  k < M (fast kernels)
   const unsigned* status;
   int cols_per_block;    // fast kernels: 8 or 16 columns per block, 0 = default
+  int prefetch;          // fast kernels: 1 = each block prefetches into L2 the spectrum of the
+                         // tile that starts about one block lifetime later (set by the launcher)
+  int prefetch_ahead;    // that distance in blocks (the launcher: resident blocks of the GPU)
 };
 
 int asg_t_default_cols(int nT, int Y, int flux);

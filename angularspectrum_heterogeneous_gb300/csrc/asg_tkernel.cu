@@ -68,6 +68,21 @@ __global__ void __launch_bounds__(256, ((PL::N >= 512 || C == 16) ? 3 : 4))
   // tile -> (x, y0); column cc: row x + (cc >= CY)*X/2, y = y0 + cc % CY
   const int tile = blockIdx.x;
   const int xq = tile / (Y / CY), y0 = CY * (tile - xq * (Y / CY));
+  if (p.prefetch_ahead > 0 && !p.in_real) {
+    // blocks start in about index order: the tile of block b + (resident
+    // blocks) starts about when this one ends, so its spectrum goes to L2 now
+    const int nt = blockIdx.x + p.prefetch_ahead;
+    if (nt < (int)gridDim.x) {
+      const int xq2 = nt / (Y / CY), y02 = CY * (nt - xq2 * (Y / CY));
+      const size_t cA = (size_t)xq2 * Y + y02, cB = cA + (size_t)X2 * Y;
+      // M + 1 planes, rows x and x + X/2: runs of CY complex (32 or 64 bytes)
+      for (int i = tid; i < 2 * (M + 1); i += nthr) {
+        const float2* a = p.spec + (size_t)(i >> 1) * ncols + ((i & 1) ? cB : cA);
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+        if (CY == 8) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 4));
+      }
+    }
+  }
   for (int i = tid; i < M; i += nthr) twM[i] = p.twM[i];
   const float2 wx = p.twX[xq];  // W_X^x of this tile's column pair
   auto col_of = [&](int cc) {
@@ -385,15 +400,24 @@ static int launch_fast_t_mode(const TParams& p, cudaStream_t st) {
   constexpr int LS = PL::PADDED + 2;
   const size_t smem = (size_t)(C * LS + M) * sizeof(float2);
   static bool attr_done[ASG_MAX_DEVICES] = {};
+  static int resident[ASG_MAX_DEVICES] = {};
   const int dev = asg_device_slot();
   if (!attr_done[dev]) {
     if (cudaFuncSetAttribute(tk_fast<PL, MODE, C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return ASG_ERR_CUDA;
+    int per_sm = 0, nsm = 0, d = 0;
+    if (cudaGetDevice(&d) == cudaSuccess &&
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, d) == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tk_fast<PL, MODE, C>, 256,
+                                                      smem) == cudaSuccess)
+      resident[dev] = per_sm * nsm;
     attr_done[dev] = true;
   }
   const int grid = (p.X / 2) * (p.Y / (C / 2));
-  tk_fast<PL, MODE, C><<<grid, 256, smem, st>>>(p);
+  TParams q = p;
+  q.prefetch_ahead = p.prefetch ? resident[dev] : 0;
+  tk_fast<PL, MODE, C><<<grid, 256, smem, st>>>(q);
   return cudaPeekAtLastError() == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
 }
 

@@ -207,6 +207,8 @@ typedef struct {
                       * between arriving at a barrier and waiting on it); the launch is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
                       * beside other heavy work on the same GPU) */
+  int t_prefetch;    /* column passes: 1 none, 2 each block prefetches into L2 the spectrum of
+                      * the tile that starts about one block lifetime later; 0 = default (1) */
   int xy_bulk;       /* HBM row loads of those kernels: 1 16-byte cp.async per lane, 2 bulk
                       * async copies (cp.async.bulk, one per row segment, mbarrier
                       * completion) in the diffraction kernel, 3 bulk copies in the
