@@ -144,7 +144,9 @@ struct TableParams {
   double kstart, kmax_t;   // cosine k-filter band
   int use_prop, use_att, obliquity, clip_negative;
   double norm;             // 1/(X*Y) folded in
-  float2* out;
+  float2* out_pa;          // propagator x attenuation (or null)
+  float2* out_p;           // propagator alone (or null)
+  float2* out_a;           // attenuation alone (or null)
 };
 int asg_launch_table(const TableParams& p, cudaStream_t st);
 int asg_launch_obl_table(const TableParams& p, float* out, cudaStream_t st);

@@ -1,7 +1,7 @@
 // Set-up kernels: FP64 construction of the per-mode multiplier tables, and
 // the small bookkeeping kernels of the march.
 //
-// Multiplier of one mode (kx, ky, bin f), built in FP64 and rounded once:
+// Multiplier of one mode (kx, ky, bin f), its phases and exponents in FP64:
 //   propagator (precalculate_mas, angular_spectrum_solver.py:396-462)
 //     kk < k^2 : mask(kk) * exp(i dz kk / (k + sqrt(k^2 - kk)))
 //                (the cancellation-free form of exp(i dz (k - kz)), :441)
@@ -17,8 +17,30 @@
 
 #include "asg_internal.h"
 
+// sin and cos of an FP64 angle: reduced to [-pi, pi] in FP64 by Cody and
+// Waite's method (2 pi split into its nearest double and the remainder), then
+// evaluated in FP32.  The angles here are below a few hundred radians, so the
+// reduction error stays near 1e-14 rad; the FP32 evaluation adds about one
+// FP32 ulp, the precision of the stored table entry.
+__device__ __forceinline__ void sincos_reduced(double ph, float* s, float* c) {
+  const double two_pi_hi = 6.283185307179586;      // nearest double to 2 pi
+  const double two_pi_lo = 2.4492935982947064e-16;  // 2 pi - two_pi_hi
+  const double n = rint(ph * 0.15915494309189535);  // ph / (2 pi), rounded
+  double r = fma(-n, two_pi_hi, ph);
+  r = fma(-n, two_pi_lo, r);
+  sincosf((float)r, s, c);
+}
+
+// All multiplier tables of one step size in one pass: per mode the propagator
+// factor P and the attenuation/KK factor A are formed once and written as
+// out_pa = P A, out_p = P, out_a = A (any output may be null).  The phases,
+// the wavenumbers and the exponents' arguments are FP64 (the propagator
+// phase in the cancellation-free form); exp and sin/cos of them are taken in
+// FP32 after an FP64 argument reduction; each entry is rounded to FP32 once
+// from the FP64 product.
 __global__ void k_build_table(TableParams p) {
   const size_t n = (size_t)p.nplanes * p.ncx * p.ncy;
+  const double kstart2 = p.kstart * p.kstart, kmax2 = p.kmax_t * p.kmax_t;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const int cy = (int)(i % p.ncy);
@@ -26,37 +48,47 @@ __global__ void k_build_table(TableParams p) {
     const int pl = (int)(i / ((size_t)p.ncy * p.ncx));
     const int f = p.f_of_plane[pl];
     const double kk = p.kx2[cx] + p.ky2[cy];
-    double re = 1.0, im = 0.0;
+    double pr = 1.0, pi = 0.0;
     if (p.use_prop) {
       if (f == 0 || 2 * f == p.nT) {
-        re = 0.0;
-        im = 0.0;
+        pr = 0.0;
+        pi = 0.0;
       } else {
         const double k = p.kt_prop[pl];
-        const double kr = sqrt(kk);
         double mask = 1.0;
-        if (kr > p.kmax_t) mask = 0.0;
-        else if (kr > p.kstart)
-          mask = 0.5 * (1.0 + cos(M_PI * (kr - p.kstart) / (p.kmax_t - p.kstart)));
-        double amp, ph;
-        if (kk < k * k) {
-          amp = 1.0;
-          ph = p.dz_prop * kk / (k + sqrt(k * k - kk));
-        } else {
-          amp = exp(-p.dz_prop * sqrt(kk - k * k));
-          ph = p.dz_prop * k;
+        if (kk > kmax2) {
+          mask = 0.0;
+        } else if (kk > kstart2) {
+          const double kr = sqrt(kk);
+          if (kr > p.kmax_t) mask = 0.0;
+          else if (kr > p.kstart)
+            mask = 0.5 * (1.0 + (double)cosf((float)(M_PI * (kr - p.kstart) /
+                                                      (p.kmax_t - p.kstart))));
         }
-        double s, c;
-        sincos(ph, &s, &c);
-        // the reference's factor 2 on the kept bins is cancelled by the real
-        // part it takes afterwards (Re(ifftn) = ifftn of (W(k)+conj W(-k))/2)
-        re = mask * amp * c;
-        im = mask * amp * s;
+        if (mask != 0.0) {
+          double amp, ph;
+          if (kk < k * k) {
+            amp = 1.0;
+            ph = p.dz_prop * kk / (k + sqrt(k * k - kk));
+          } else {
+            amp = (double)expf((float)(-p.dz_prop * sqrt(kk - k * k)));
+            ph = p.dz_prop * k;
+          }
+          float sn, cs;
+          sincos_reduced(ph, &sn, &cs);
+          // the reference's factor 2 on the kept bins is cancelled by the real
+          // part it takes afterwards (Re(ifftn) = ifftn of (W(k)+conj W(-k))/2)
+          pr = mask * amp * (double)cs;
+          pi = mask * amp * (double)sn;
+        } else {
+          pr = 0.0;
+          pi = 0.0;
+        }
       }
     }
+    double ar = 1.0, ai = 0.0;
     if (p.use_att) {
       const double km = p.km_att[pl];
-      double ar = 1.0, ai = 0.0;
       if (km != 0.0) {
         const double br = -p.alpha[pl] * p.dz_att;
         const double bi = -p.astar[pl] * p.dz_att;
@@ -71,23 +103,23 @@ __global__ void k_build_table(TableParams p) {
           }
         }
         if (prop) {
-          const double mag = exp(br * obl);
-          double s, c;
-          sincos(bi * obl, &s, &c);
-          ar = mag * c;
-          ai = mag * s;
+          const double mag = (double)expf((float)(br * obl));
+          float sn, cs;
+          sincos_reduced(bi * obl, &sn, &cs);
+          ar = mag * (double)cs;
+          ai = mag * (double)sn;
         }
       }
       if (p.clip_negative && ar < 0.0) {
         ar = 0.0;
         ai = 0.0;
       }
-      const double nr = re * ar - im * ai;
-      const double ni = re * ai + im * ar;
-      re = nr;
-      im = ni;
     }
-    p.out[i] = make_float2((float)(re * p.norm), (float)(im * p.norm));
+    const double nrm = p.norm;
+    if (p.out_pa != nullptr)
+      p.out_pa[i] = make_float2((float)((pr * ar - pi * ai) * nrm), (float)((pr * ai + pi * ar) * nrm));
+    if (p.out_p != nullptr) p.out_p[i] = make_float2((float)(pr * nrm), (float)(pi * nrm));
+    if (p.out_a != nullptr) p.out_a[i] = make_float2((float)(ar * nrm), (float)(ai * nrm));
   }
 }
 
