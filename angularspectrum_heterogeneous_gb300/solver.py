@@ -287,14 +287,20 @@ def host_empty(shape, dtype=np.float32):
     costs the OS zeroing and, for the device copy, page-locking of every
     page on each call; a cached pinned block costs neither, and the copy runs
     at the host link's full rate.  Plain numpy memory if no device is there."""
+    global HOST_EMPTY_FALLBACKS
     try:
         import torch
         if torch.cuda.is_available():
             td = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}
             return torch.empty(tuple(shape), dtype=td[np.dtype(dtype)], pin_memory=True).numpy()
-    except (ImportError, KeyError, RuntimeError):
-        pass
+    except (ImportError, KeyError, RuntimeError) as e:
+        HOST_EMPTY_FALLBACKS += 1
+        LAST_SOLVE_TIMINGS["host_alloc_fallback"] = str(e)[:200]
     return np.empty(shape, dtype)
+
+
+# allocations host_empty could not page-lock (plain numpy memory instead)
+HOST_EMPTY_FALLBACKS = 0
 
 
 def _torch_view(ptr, shape):
@@ -451,6 +457,7 @@ def angular_spectrum_solve(
         raise ValueError("initial_field must be (nX, nY, nT)")
     nX, nY, nT = u0.shape
     t_start = _time.perf_counter()
+    LAST_SOLVE_TIMINGS.clear()
     plan, dz, steps = _prepared_plan(u0, params)
     try:
         cb = None
@@ -463,10 +470,10 @@ def angular_spectrum_solve(
         t_run = _time.perf_counter()
         out = plan.outputs()
         t_out = _time.perf_counter()
-        LAST_SOLVE_TIMINGS.clear()
         LAST_SOLVE_TIMINGS.update(plan_s=t_plan - t_start, run_s=t_run - t_plan,
                                   march_device_s=plan.last_run_ms() / 1e3,
-                                  outputs_s=t_out - t_run)
+                                  outputs_s=t_out - t_run,
+                                  host_alloc_fallbacks=HOST_EMPTY_FALLBACKS)
         if verbose:
             z = 0.0
             for cc, d in enumerate(steps):
