@@ -648,6 +648,14 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
     wxs[i] = (p.epi & EPI_SUPERABS) ? p.sa_wx[i] : 0.f;
   }
   float2* S = p.l2_scratch + (size_t)cid * X * Y;     // rows of a, then rows of b
+  // chunks of the x-edge walk that hold Engquist-Majda weights (fixed per launch)
+  __shared__ unsigned char x_chunk_any[NT / YR];
+  __syncthreads();
+  if (tid < NT / YR) {
+    bool any = false;
+    for (int x = tid * CHUNK; x < (tid + 1) * CHUNK; ++x) any |= wxs[x] != 0.f;
+    x_chunk_any[tid] = any ? 1 : 0;
+  }
   const bool fw = (p.epi & EPI_FREQW) != 0, sa = (p.epi & EPI_SUPERABS) != 0;
   const float st = p.sa_strength;
 
@@ -799,11 +807,8 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         const int c = tid % YR, x0 = (tid / YR) * CHUNK;
         const float2 lo = x0 > 0 ? tile[(x0 - 1) * TS + c] : make_float2(0.f, 0.f);
         const float2 hi = x0 + CHUNK < X ? tile[(x0 + CHUNK) * TS + c] : make_float2(0.f, 0.f);
-        bool any = false;
-#pragma unroll
-        for (int x = x0; x < x0 + CHUNK; ++x) any |= wxs[x] != 0.f;
         __syncthreads();
-        if (any) {
+        if (x_chunk_any[tid / YR]) {
           float2 prev = lo, cur = tile[x0 * TS + c];
 #pragma unroll 8
           for (int x = x0; x < x0 + CHUNK; ++x) {
@@ -853,65 +858,104 @@ __global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
         stepB_smem<PY, true>(buf + (warp + NW * j) * RS, ka);
       }
       __syncwarp();
-      for (int i = lane; i < RPW * PY::N2; i += 32) {
-        const int j = i / PY::N2, b = i - j * PY::N2;
-        stepA_inv_smem<PY>(buf + (warp + NW * j) * RS, b, tw_y);
-      }
-      __syncwarp();
-#pragma unroll 1
-      for (int j = 0; j < RPW; ++j) {
-        const int r = warp + NW * j;
-        const int x = h * Xs + rank * R + r;
-        const float2* row = buf + r * RS;
-        float2* grow = p.spec + ((size_t)plane * X + x) * Y;
-        if (!epi) {
-          for (int y = lane; y < Y; y += 32) grow[y] = row[PY::pos(y)];
-          continue;
+      // the epilogue of 32 consecutive outputs y = y0 + lane of row x: damping
+      // y factor, Engquist-Majda y edges (neighbours by shuffles; lane 31's
+      // right neighbour `nxt` is the undamped value at y0 + 32, lane 0's left
+      // one the damped value at y0 - 1 carried in prev_last), screens, store
+      auto epilogue32 = [&](int x, int y0, float2 cur, float2 nxt, float2& prev_last,
+                            float2* grow) {
+        const int y = y0 + lane;
+        if (fw) cur = cscale(cur, gys[y]);
+        float2 res = cur;
+        if (sa) {
+          float2 left, right;
+          left.x = __shfl_up_sync(0xffffffffu, cur.x, 1);
+          left.y = __shfl_up_sync(0xffffffffu, cur.y, 1);
+          right.x = __shfl_down_sync(0xffffffffu, cur.x, 1);
+          right.y = __shfl_down_sync(0xffffffffu, cur.y, 1);
+          if (lane == 0) left = prev_last;
+          if (lane == 31 && y + 1 < Y) right = fw ? cscale(nxt, gys[y + 1]) : nxt;
+          const float w = wys[y];
+          if (w != 0.f) {
+            float2 d;
+            if (y == 0) d = cscale(csub(right, cur), p.sa_invdy);
+            else if (y == Y - 1) d = cscale(csub(cur, left), p.sa_invdy);
+            else d = cscale(csub(right, left), p.sa_inv2dy);
+            const float2 cd = make_float2(cf * d.y, -cf * d.x);
+            const float2 P = (y < Y / 2) ? make_float2(0.5f * (cur.x + cd.x), 0.5f * (cur.y + cd.y))
+                                         : make_float2(0.5f * (cur.x - cd.x), 0.5f * (cur.y - cd.y));
+            res = make_float2(cur.x - st * w * P.x, cur.y - st * w * P.y);
+          }
+          prev_last.x = __shfl_sync(0xffffffffu, cur.x, 31);
+          prev_last.y = __shfl_sync(0xffffffffu, cur.y, 31);
         }
-        float2 prev_last = make_float2(0.f, 0.f);  // value at y0-1 (damped, not corrected)
-        for (int y0 = 0; y0 < Y; y0 += 32) {
-          const int y = y0 + lane;
-          float2 cur = row[PY::pos(y)];
-          if (fw) cur = cscale(cur, gys[y]);
-          float2 res = cur;
-          if (sa) {
-            float2 left, right;
-            left.x = __shfl_up_sync(0xffffffffu, cur.x, 1);
-            left.y = __shfl_up_sync(0xffffffffu, cur.y, 1);
-            right.x = __shfl_down_sync(0xffffffffu, cur.x, 1);
-            right.y = __shfl_down_sync(0xffffffffu, cur.y, 1);
-            if (lane == 0) left = prev_last;
-            if (lane == 31 && y + 1 < Y) {
-              right = row[PY::pos(y + 1)];
-              if (fw) right = cscale(right, gys[y + 1]);
-            }
-            const float w = wys[y];
-            if (w != 0.f) {
-              float2 d;
-              if (y == 0) d = cscale(csub(right, cur), p.sa_invdy);
-              else if (y == Y - 1) d = cscale(csub(cur, left), p.sa_invdy);
-              else d = cscale(csub(right, left), p.sa_inv2dy);
-              const float2 cd = make_float2(cf * d.y, -cf * d.x);
-              const float2 P = (y < Y / 2) ? make_float2(0.5f * (cur.x + cd.x), 0.5f * (cur.y + cd.y))
-                                           : make_float2(0.5f * (cur.x - cd.x), 0.5f * (cur.y - cd.y));
-              res = make_float2(cur.x - st * w * P.x, cur.y - st * w * P.y);
-            }
-            prev_last.x = __shfl_sync(0xffffffffu, cur.x, 31);
-            prev_last.y = __shfl_sync(0xffffffffu, cur.y, 31);
+        for (int k = 0; k < p.nscreens; ++k) {
+          const float fs = p.screen_fscale[plane];
+          const ScreenDev sc = p.screens[k];
+          const size_t g = (size_t)x * Y + y;
+          float sn, cs;
+          sincosf(sc.phase[g] * fs, &sn, &cs);
+          res = cmul(res, make_float2(cs, -sn));
+          if (sc.amp != nullptr) {
+            const float a = fminf(fmaxf(sc.amp[g], 1e-6f), 1.0f);
+            res = cscale(res, exp2f(fs * log2f(a)));
           }
-          for (int k = 0; k < p.nscreens; ++k) {
-            const float fs = p.screen_fscale[plane];
-            const ScreenDev sc = p.screens[k];
-            const size_t g = (size_t)x * Y + y;
-            float sn, cs;
-            sincosf(sc.phase[g] * fs, &sn, &cs);
-            res = cmul(res, make_float2(cs, -sn));
-            if (sc.amp != nullptr) {
-              const float a = fminf(fmaxf(sc.amp[g], 1e-6f), 1.0f);
-              res = cscale(res, exp2f(fs * log2f(a)));
-            }
+        }
+        grow[y] = res;
+      };
+      if constexpr (PY::N2 == 32) {
+        // lane b's inverse step-A outputs are y = b + 32 a: the epilogue runs
+        // on them in registers, row by row (no store and reload of the row)
+#pragma unroll 1
+        for (int j = 0; j < RPW; ++j) {
+          const int r = warp + NW * j;
+          const int x = h * Xs + rank * R + r;
+          const float2* row = buf + r * RS;
+          float2* grow = p.spec + ((size_t)plane * X + x) * Y;
+          const int b = lane;
+          float2 v[PY::N1];
+          v[0] = row[PY::pos(b)];
+#pragma unroll
+          for (int ka = 1; ka < PY::N1; ++ka) v[ka] = cmulc(row[PY::pos(b + 32 * ka)], tw_y[b * ka]);
+          dft<PY::N1, true>(v);
+          if (!epi) {
+#pragma unroll
+            for (int a = 0; a < PY::N1; ++a) grow[b + 32 * a] = v[a];
+            continue;
           }
-          grow[y] = res;
+          float2 prev_last = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int a = 0; a < PY::N1; ++a) {
+            float2 nxt = make_float2(0.f, 0.f);
+            if (a + 1 < PY::N1 && sa) {
+              nxt.x = __shfl_sync(0xffffffffu, v[a + 1 < PY::N1 ? a + 1 : a].x, 0);
+              nxt.y = __shfl_sync(0xffffffffu, v[a + 1 < PY::N1 ? a + 1 : a].y, 0);
+            }
+            epilogue32(x, 32 * a, v[a], nxt, prev_last, grow);
+          }
+        }
+      } else {
+        for (int i = lane; i < RPW * PY::N2; i += 32) {
+          const int j = i / PY::N2, b = i - j * PY::N2;
+          stepA_inv_smem<PY>(buf + (warp + NW * j) * RS, b, tw_y);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int j = 0; j < RPW; ++j) {
+          const int r = warp + NW * j;
+          const int x = h * Xs + rank * R + r;
+          const float2* row = buf + r * RS;
+          float2* grow = p.spec + ((size_t)plane * X + x) * Y;
+          if (!epi) {
+            for (int y = lane; y < Y; y += 32) grow[y] = row[PY::pos(y)];
+            continue;
+          }
+          float2 prev_last = make_float2(0.f, 0.f);  // value at y0-1 (damped, not corrected)
+          for (int y0 = 0; y0 < Y; y0 += 32) {
+            const int y = y0 + lane;
+            const float2 nxt = (lane == 31 && y + 1 < Y) ? row[PY::pos(y + 1)] : make_float2(0.f, 0.f);
+            epilogue32(x, y0, row[PY::pos(y)], nxt, prev_last, grow);
+          }
         }
       }
       __syncwarp();
