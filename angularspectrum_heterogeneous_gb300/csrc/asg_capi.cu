@@ -72,11 +72,30 @@ static int h2d(T* d, const T* h, size_t n, cudaStream_t st) {
 // host link's rate instead of going through the driver's staging buffers, and
 // unlocked again once the copy is done; a buffer that cannot be registered
 // (already registered, for one) takes the pageable copy.
+// Whether the current device reads pageable host memory through the host's page
+// tables (address translation services, as on Grace-based systems): copies from
+// and to pageable memory then run at the link's full rate and page-locking a
+// buffer first only costs time.
+static bool pageable_is_direct() {
+  static int cached[ASG_MAX_DEVICES] = {};  // 0 unknown, 1 no, 2 yes
+  const int dev = asg_device_slot();
+  if (cached[dev] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+        cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 0;
+    }
+    cached[dev] = v ? 2 : 1;
+  }
+  return cached[dev] == 2;
+}
+
 static int copy_host(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind,
                      cudaStream_t st) {
   void* host = kind == cudaMemcpyHostToDevice ? const_cast<void*>(src) : dst;
   bool reg = false;
-  if (bytes >= ((size_t)32 << 20)) {
+  if (bytes >= ((size_t)32 << 20) && !pageable_is_direct()) {
     reg = cudaHostRegister(host, bytes, cudaHostRegisterDefault) == cudaSuccess;
     if (!reg) (void)cudaGetLastError();
   }

@@ -305,7 +305,7 @@ def run_gpu_arm(args):
     value = world * V * args.steps / (ms / 1e3)
 
     # e2e: public API, host buffers in and out, K steps; the input field in
-    # page-locked host memory, one untimed call first (host allocator warm-up)
+    # page-locked host memory, two untimed calls first (host allocator warm-up)
     e2e_s, h2d, d2h = float("nan"), 0, 0
     e2e_phases = None
     if not args.no_e2e:
@@ -314,8 +314,9 @@ def run_gpu_arm(args):
         u_host[...] = u0
         p2 = workload_params()
         p2.propDist = args.steps * dz
-        warm = angular_spectrum_solve(u_host, p2, verbose=False)
-        del warm  # its pinned blocks go back to the cache for the timed call
+        for _ in range(2):  # host allocator warm-up: the pinned blocks return to its cache
+            warm = angular_spectrum_solve(u_host, p2, verbose=False)
+            del warm
         torch.cuda.synchronize()
         t0 = time.time()
         out = angular_spectrum_solve(u_host, p2, verbose=False)
