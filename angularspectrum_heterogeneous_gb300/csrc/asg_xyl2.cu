@@ -181,8 +181,20 @@ ASG_DEV bool group_barrier(unsigned* cnt, unsigned target, unsigned* status, int
 
 }  // namespace
 
+// Planes up to 384 wide run three blocks per SM (80 registers without spills;
+// the diffraction kernel then reads its twiddle and class tables through L1 to
+// keep its shared memory to the row buffer; the closing kernel fits as it is):
+// 4-7 % faster than two.  512-wide planes keep two blocks, the diffraction
+// kernel's tables in shared memory (at 80 registers their 32-point row
+// transform spills, and the closing kernel's shared memory allows two).
+template <class PY>
+struct L2Shape {
+  static constexpr bool kTablesInSmem = PY::N >= 512;
+  static constexpr int kMinBlocks = kTablesInSmem ? 2 : 3;
+};
+
 template <class PY, class PX, int R, int NT>
-__global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
+__global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2(XYParams p) {
   constexpr int Y = PY::N, RS = PY::PADDED;
   constexpr int Xs = PX::N;
   constexpr int NW = NT / 32;
@@ -197,11 +209,15 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   float2* buf = reinterpret_cast<float2*>(smraw);       // rows [R][RS] or tile [Xs][TS]
   __shared__ float red[2][NW];
 
+  constexpr bool TS_SMEM = L2Shape<PY>::kTablesInSmem;
   const int nbuf = p.l2_buf_elems;   // max(R*RS, Xs*TS), set by the host
-  float2* tw_y = buf + nbuf;
-  float2* tw_x = tw_y + Y;
-  int* clsy = reinterpret_cast<int*>(tw_x + Xs);
-  int* clsx = clsy + Y;               // [nsub][Xs] by x slot of the Xs-point FFT
+  float2* tw_y_s = buf + nbuf;
+  float2* tw_x_s = tw_y_s + Y;
+  int* clsy_s = reinterpret_cast<int*>(tw_x_s + Xs);
+  int* clsx_s = clsy_s + Y;           // [nsub][Xs] by x slot of the Xs-point FFT
+  const float2* tw_y = TS_SMEM ? tw_y_s : p.twY;
+  const int* clsy = TS_SMEM ? clsy_s : p.cls_y;
+  const int* clsx = TS_SMEM ? clsx_s : p.l2_cls_x;
 
   cg::cluster_group cl = cg::this_cluster();
   const bool coop = p.coop != 0;
@@ -234,12 +250,16 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
   unsigned row_phase = 0;
   bool row_pending = false;
 
-  for (int i = tid; i < Y; i += NT) {
-    tw_y[i] = p.twY[i];
-    clsy[i] = p.cls_y[i];
+  if constexpr (TS_SMEM) {
+    for (int i = tid; i < Y; i += NT) {
+      tw_y_s[i] = p.twY[i];
+      clsy_s[i] = p.cls_y[i];
+    }
+    for (int i = tid; i < Xs; i += NT) tw_x_s[i] = p.twX[i * nsub];  // W_Xs^i
+    for (int i = tid; i < nsub * Xs; i += NT) clsx_s[i] = p.l2_cls_x[i];
   }
-  for (int i = tid; i < Xs; i += NT) tw_x[i] = p.twX[i * nsub];  // W_Xs^i
-  for (int i = tid; i < nsub * Xs; i += NT) clsx[i] = p.l2_cls_x[i];
+  const int nsub_l = nsub;
+  auto tw_x = [&](int i) { return TS_SMEM ? tw_x_s[i] : __ldg(p.twX + i * nsub_l); };
   float2* scratch0 = p.l2_scratch + (size_t)cid * 2 * Xs * Y;
 
   auto zero_plane = [&](int q) {
@@ -328,7 +348,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       dft<PX::N1, false>(v);
       buf[b * TS + c] = v[0];
 #pragma unroll
-      for (int ka = 1; ka < PX::N1; ++ka) buf[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x[b * ka]);
+      for (int ka = 1; ka < PX::N1; ++ka) buf[(b + PX::N2 * ka) * TS + c] = cmul(v[ka], tw_x(b * ka));
     }
     __syncthreads();
     float psum = 0.f, pden = 0.f;
@@ -392,7 +412,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
       float2 v[PX::N1];
       v[0] = buf[b * TS + c];
 #pragma unroll
-      for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(buf[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
+      for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(buf[(b + PX::N2 * ka) * TS + c], tw_x(b * ka));
       dft<PX::N1, true>(v);
 #pragma unroll
       for (int a = 0; a < PX::N1; ++a) buf[(b + PX::N2 * a) * TS + c] = v[a];
@@ -586,7 +606,7 @@ __global__ void __launch_bounds__(NT, 2) xy_l2(XYParams p) {
 // :352-390, :1494-1518)
 // ---------------------------------------------------------------------------
 template <class PY, class PX, int R, int NT>
-__global__ void __launch_bounds__(NT, 2) xy_l2c(XYParams p) {
+__global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2c(XYParams p) {
   constexpr int Y = PY::N, RS = PY::PADDED;
   constexpr int Xs = PX::N, X = 2 * Xs;
   constexpr int NW = NT / 32;
@@ -1039,7 +1059,10 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
   const int Yc = Yn / p.G;
   const int nbuf = (R * PY::PADDED > Xn * Yc) ? R * PY::PADDED : Xn * Yc;
   p.l2_buf_elems = nbuf;
-  const size_t smem = (size_t)(nbuf + Yn + Xn) * sizeof(float2) + (size_t)(Yn + 2 * Xn) * sizeof(int);
+  const size_t smem =
+      L2Shape<PY>::kTablesInSmem
+          ? (size_t)(nbuf + Yn + Xn) * sizeof(float2) + (size_t)(Yn + 2 * Xn) * sizeof(int)
+          : (size_t)nbuf * sizeof(float2);
   auto kern = xy_l2<PY, PX, R, NT>;
   static int max_clusters_dev[ASG_MAX_DEVICES], cached_G_dev[ASG_MAX_DEVICES];
   static bool init_dev[ASG_MAX_DEVICES] = {};
