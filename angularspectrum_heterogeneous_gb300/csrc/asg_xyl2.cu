@@ -181,20 +181,22 @@ ASG_DEV bool group_barrier(unsigned* cnt, unsigned target, unsigned* status, int
 
 }  // namespace
 
-// Planes up to 384 wide run three blocks per SM (80 registers without spills;
-// the diffraction kernel then reads its twiddle and class tables through L1 to
-// keep its shared memory to the row buffer; the closing kernel fits as it is):
-// 4-7 % faster than two.  512-wide planes keep two blocks, the diffraction
-// kernel's tables in shared memory (at 80 registers their 32-point row
-// transform spills, and the closing kernel's shared memory allows two).
-template <class PY>
+// Blocks per SM.  With 8-warp blocks, planes up to 384 wide run three per SM
+// (80 registers without spills; the diffraction kernel then reads its twiddle
+// and class tables through L1 to keep its shared memory to the row buffer; the
+// closing kernel fits as it is): 4-7 % faster than two.  512-wide planes keep
+// two, the diffraction kernel's tables in shared memory (at 80 registers their
+// 32-point row transform spills, and the closing kernel's shared memory allows
+// two).  The diffraction kernel's 4-warp blocks of a cooperative launch (8
+// rows per CTA) run twice as many blocks per SM with the same registers.
+template <class PY, int NT>
 struct L2Shape {
   static constexpr bool kTablesInSmem = PY::N >= 512;
-  static constexpr int kMinBlocks = kTablesInSmem ? 2 : 3;
+  static constexpr int kMinBlocks = (kTablesInSmem ? 2 : 3) * (NT == 128 ? 2 : 1);
 };
 
 template <class PY, class PX, int R, int NT>
-__global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2(XYParams p) {
+__global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2(XYParams p) {
   constexpr int Y = PY::N, RS = PY::PADDED;
   constexpr int Xs = PX::N;
   constexpr int NW = NT / 32;
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2(XYParams p)
   float2* buf = reinterpret_cast<float2*>(smraw);       // rows [R][RS] or tile [Xs][TS]
   __shared__ float red[2][NW];
 
-  constexpr bool TS_SMEM = L2Shape<PY>::kTablesInSmem;
+  constexpr bool TS_SMEM = L2Shape<PY, NT>::kTablesInSmem;
   const int nbuf = p.l2_buf_elems;   // max(R*RS, Xs*TS), set by the host
   float2* tw_y_s = buf + nbuf;
   float2* tw_x_s = tw_y_s + Y;
@@ -606,7 +608,7 @@ __global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2(XYParams p)
 // :352-390, :1494-1518)
 // ---------------------------------------------------------------------------
 template <class PY, class PX, int R, int NT>
-__global__ void __launch_bounds__(NT, L2Shape<PY>::kMinBlocks) xy_l2c(XYParams p) {
+__global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2c(XYParams p) {
   constexpr int Y = PY::N, RS = PY::PADDED;
   constexpr int Xs = PX::N, X = 2 * Xs;
   constexpr int NW = NT / 32;
@@ -1049,18 +1051,20 @@ static int launch_groups(K kern, const XYParams& p, cudaLaunchConfig_t cfg, int 
   return e == cudaSuccess ? ASG_OK : ASG_ERR_CUDA;
 }
 
-template <int Yn, int Xn>
+// R rows per CTA and NT threads per block; the plan's group size p.G is that
+// of 16-row CTAs (the cluster shape), the launch uses Xn / R.
+template <int Yn, int Xn, int R, int NT>
 static int launch_l2(const XYParams& pin, cudaStream_t st) {
   using PY = FastPlan<Yn>;
   using PX = FastPlan<Xn>;
-  constexpr int R = 16, NT = 256;
   XYParams p = pin;
-  if (p.G != Xn / R) return ASG_ERR_SHAPE;
+  if (p.G != Xn / 16) return ASG_ERR_SHAPE;
+  p.G = Xn / R;
   const int Yc = Yn / p.G;
   const int nbuf = (R * PY::PADDED > Xn * Yc) ? R * PY::PADDED : Xn * Yc;
   p.l2_buf_elems = nbuf;
   const size_t smem =
-      L2Shape<PY>::kTablesInSmem
+      L2Shape<PY, NT>::kTablesInSmem
           ? (size_t)(nbuf + Yn + Xn) * sizeof(float2) + (size_t)(Yn + 2 * Xn) * sizeof(int)
           : (size_t)nbuf * sizeof(float2);
   auto kern = xy_l2<PY, PX, R, NT>;
@@ -1094,7 +1098,9 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     cfg.gridDim = dim3(p.G * 1024, 1, 1);
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) n = 1;
+    // groups of more than 16 CTAs run only as cooperative launches
+    if (p.G > 16 || cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0)
+      n = 1;
     max_clusters = n;
     max_groups = coop_max_groups(kern, NT, smem, p.G);
     cached_G = p.G;
@@ -1103,14 +1109,28 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
   return launch_groups(kern, p, cfg, p.coop ? max_groups : max_clusters, nq, st);
 }
 
+// Cooperative launches of the transform (not the power sums, which keep the
+// summation order of the cluster shape) run 8-row CTAs of 4 warps from
+// 256-wide planes up: 512 x 512 x 1024 xy_A/xy_B 1.33 -> 1.25 ms against
+// 16-row CTAs of 8 warps (more blocks per SM to overlap each other's load
+// waits; 4-row CTAs of 2 warps were slower again).  Thread-block clusters hold
+// at most 16 CTAs and keep 16 rows per CTA.
+template <int Yn, int Xn>
+static int launch_l2_mode(const XYParams& p, cudaStream_t st) {
+  if constexpr (Yn >= 256) {
+    if (p.coop && !p.power_only) return launch_l2<Yn, Xn, 8, 128>(p, st);
+  }
+  return launch_l2<Yn, Xn, 16, 256>(p, st);
+}
+
 int asg_launch_xy_l2(const XYParams& p, cudaStream_t st) {
   const int Xs = p.X / p.nsub;
   switch (p.Y) {
-    case 128: return Xs == 32 ? launch_l2<128, 32>(p, st) : launch_l2<128, 64>(p, st);
-    case 192: return launch_l2<192, 96>(p, st);
-    case 256: return launch_l2<256, 128>(p, st);
-    case 384: return launch_l2<384, 192>(p, st);
-    case 512: return launch_l2<512, 256>(p, st);
+    case 128: return Xs == 32 ? launch_l2_mode<128, 32>(p, st) : launch_l2_mode<128, 64>(p, st);
+    case 192: return launch_l2_mode<192, 96>(p, st);
+    case 256: return launch_l2_mode<256, 128>(p, st);
+    case 384: return launch_l2_mode<384, 192>(p, st);
+    case 512: return launch_l2_mode<512, 256>(p, st);
     default: return ASG_ERR_SHAPE;
   }
 }
