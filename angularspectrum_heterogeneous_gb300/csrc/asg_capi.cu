@@ -227,7 +227,8 @@ struct asg_plan {
   int t_cols[3] = {0, 0, 0};  // columns per block: flux, taper-only, statistics column passes
   int xy_clusters = 0;        // resident-cluster cap of the L2 plane kernel (0 = all)
   int xy_clusters_c = 0;      // the same for the closing-stage kernel
-  int xy_bulk = 1;            // HBM row loads of the L2 plane kernels (XYParams::bulk_rows)
+  int xy_bulk = 1;            // HBM row loads of the L2 plane kernels (XYParams::bulk_rows);
+                              // set from default_bulk() at plan creation
   int t_prefetch = 0;         // column passes: L2 prefetch of a later tile (TParams::prefetch)
   int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
                               // 1 thread-block cluster, 2 counters in a cooperative launch
@@ -302,6 +303,12 @@ struct asg_plan {
   std::vector<cudaEvent_t> ev_pool;
   std::vector<int> ev_kind;  // kind of event pair i (events 2i, 2i+1)
 };
+
+// Default HBM row loads of the plane kernels: 16-byte cp.async where the
+// diffraction kernel runs 8-row CTAs in a cooperative launch (from 256-wide
+// planes: 1-4 % faster than bulk copies there), bulk copies in the diffraction
+// kernel otherwise.
+static int default_bulk(const asg_plan* p) { return (p->l2 && p->Y >= 256) ? 0 : 1; }
 
 // launch accounting around one kernel launch of `kind`
 struct KScope {
@@ -415,6 +422,7 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
   p->tfast = asg_t_fast_supported(T) && X % 2 == 0 && Y % 4 == 0;
   int Gs = 0, Gl = 0;
   p->l2 = p->tfast && asg_xy_l2_supported(X, Y, 2, &Gl);
+  p->xy_bulk = default_bulk(p);
   p->split = p->l2 || (p->tfast && asg_xy_split_supported(X, Y, &Gs));
   p->xyfast = p->split || asg_xy_fast_supported(X, Y, &p->G);
   p->nsub = 1;
@@ -887,13 +895,15 @@ static TParams tparams(asg_plan* p) {
 // (3; 3 % faster than 2 at 512-wide planes), for groups of 12 and 16 CTAs (large clusters leave SMs
 // idle, since a cluster must fit in one GPC: 14 clusters of 16 are resident on
 // a GB300, 224 of 304 CTA slots; measured 20 % faster at 512-wide planes, 2 %
-// at 384), thread-block clusters for smaller groups, which pack well and
-// measure faster (6 % at 256), and inside a batch, whose plans run side by side.
+// at 384) and from 256-wide planes up, where a cooperative launch runs the
+// diffraction kernel with 8-row CTAs (256 x 256 x 1024: 2.02 -> 1.90 ms per
+// step against clusters); thread-block clusters for smaller planes, which pack
+// well, and inside a batch, whose plans run side by side.
 static int xy_sync_of(const asg_plan* p) {
   if (!p->l2) return 0;
   if (p->batch_refs > 0) return 1;
   if (p->xy_sync != 0) return p->xy_sync;
-  return p->G >= 12 ? 3 : 1;
+  return (p->G >= 12 || p->Y >= 256) ? 3 : 1;
 }
 
 static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
@@ -1731,7 +1741,7 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
   p->xy_clusters = t->xy_clusters;
   p->xy_clusters_c = t->xy_clusters_closing;
   p->xy_sync = t->xy_sync;
-  p->xy_bulk = t->xy_bulk == 0 ? 1 : t->xy_bulk - 1;
+  p->xy_bulk = t->xy_bulk == 0 ? default_bulk(p) : t->xy_bulk - 1;
   p->t_prefetch = t->t_prefetch == 0 ? 0 : t->t_prefetch - 1;
   p->gen++;
   return ASG_OK;

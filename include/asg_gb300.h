@@ -212,7 +212,8 @@ typedef struct {
   int xy_bulk;       /* HBM row loads of those kernels: 1 16-byte cp.async per lane, 2 bulk
                       * async copies (cp.async.bulk, one per row segment, mbarrier
                       * completion) in the diffraction kernel, 3 bulk copies in the
-                      * closing-stage kernel too; 0 = default (2) */
+                      * closing-stage kernel too; 0 = default (1 from 256-wide planes,
+                      * where cooperative launches run 8-row CTAs, else 2) */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of
