@@ -69,11 +69,20 @@ struct PaddedColumn {
   ASG_DEV int idx(int t) const { int j = t >> 1; return 2 * (j + 2 * (j / N2)) + (t & 1); }
   ASG_DEV float get(int t) const { return base[idx(t)]; }
   ASG_DEV void set(int t, float v) const { base[idx(t)] = v; }
+  // Runs of CH samples starting at multiples of CH lie inside one padded row
+  // (2 N2 samples) and start on a 16-byte boundary (the rows and their pads
+  // are multiples of four floats): such a run is a contiguous float4 array.
+  template <int CH>
+  static constexpr bool kVecRun = (2 * N2) % CH == 0 && CH % 4 == 0;
+  ASG_DEV float4* run4(int t0) const { return reinterpret_cast<float4*>(base + idx(t0)); }
 };
 struct PlainColumn {
   float* base;
   ASG_DEV float get(int t) const { return base[t]; }
   ASG_DEV void set(int t, float v) const { base[t] = v; }
+  template <int CH>
+  static constexpr bool kVecRun = false;
+  ASG_DEV float4* run4(int t0) const { return reinterpret_cast<float4*>(base + t0); }
 };
 // Skewed copy of a column for the chunked KT step (lane l owns samples
 // 32l .. 32l+31): one pad word per 32 samples puts the 32 lanes' i-th samples
@@ -371,17 +380,32 @@ ASG_DEV void kt_column_step_chunk(const Col& col, int nT, float ndt, float dz, u
 // samples); the lane recomputes s1 at t0-2, t0-1 (a short prologue).  The
 // column ends t = 0 and nT-1 keep zero slope and zero rhs, as in the reference
 // (:758-839).
+//
+// When the lane's run is a contiguous, 16-byte aligned float4 array
+// (Col::kVecRun), it is read and written four samples at a time: the 32
+// lanes' runs start in only 8 distinct shared-memory banks, so scalar accesses
+// cost four wavefronts each, while a warp's float4 access is 4 wavefronts for
+// four samples.  The arithmetic is the same.
 template <int CH, bool MC, class Col>
 ASG_DEV void kt_step_stream(const Col& col, float ndt, float dz, unsigned mask) {
   static_assert(CH >= 4, "four halo samples per side");
+  constexpr bool VEC = Col::template kVecRun<CH>;
   const int lane = threadIdx.x & 31;
   const int t0 = lane * CH;
   const bool nf = lane != 0, nl = lane != 31;  // run not at the column start / end
   const float c = -ndt * dz;
   auto sl = [](float a, float b, float d) { return kt_slope<MC>(a, b, d); };
-  const float a0 = col.get(t0), a1 = col.get(t0 + 1), a2 = col.get(t0 + 2), a3 = col.get(t0 + 3);
-  const float z0 = col.get(t0 + CH - 4), z1 = col.get(t0 + CH - 3), z2 = col.get(t0 + CH - 2),
-              z3 = col.get(t0 + CH - 1);
+  float4* run = VEC ? col.run4(t0) : nullptr;
+  float a0, a1, a2, a3, z0, z1, z2, z3;
+  if constexpr (VEC) {
+    const float4 h = run[0], e = run[CH / 4 - 1];
+    a0 = h.x; a1 = h.y; a2 = h.z; a3 = h.w;
+    z0 = e.x; z1 = e.y; z2 = e.z; z3 = e.w;
+  } else {
+    a0 = col.get(t0); a1 = col.get(t0 + 1); a2 = col.get(t0 + 2); a3 = col.get(t0 + 3);
+    z0 = col.get(t0 + CH - 4); z1 = col.get(t0 + CH - 3); z2 = col.get(t0 + CH - 2);
+    z3 = col.get(t0 + CH - 1);
+  }
   float hm4 = __shfl_up_sync(mask, z0, 1), hm3 = __shfl_up_sync(mask, z1, 1);
   float hm2 = __shfl_up_sync(mask, z2, 1), hm1 = __shfl_up_sync(mask, z3, 1);
   float hp[4] = {__shfl_down_sync(mask, a0, 1), __shfl_down_sync(mask, a1, 1),
@@ -405,10 +429,24 @@ ASG_DEV void kt_step_stream(const Col& col, float ndt, float dz, unsigned mask) 
   float q0 = nf ? sl(r_m1, r0, r1) : 0.f;        // slope of s1 at t
   float G = kt_fh(r_m1 + 0.5f * qm1, r0 - 0.5f * q0);  // flux of s1 at t-1/2
   float w0 = a0, w1 = a1, w2 = a2, w3 = a3;      // u[t .. t+3]
+  // VEC: one float4 holds the chunk of samples 4q+4 .. 4q+7 (read at i = 4q)
+  // and, component by component as each is used, the new samples 4q .. 4q+3
+  // (written back at i = 4q+3)
+  float4 ahead = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
   for (int i = 0; i < CH; ++i) {
     const int t = t0 + i;
-    const float u4 = (i + 4 < CH) ? col.get(t + 4) : hp[(i + 4 - CH) & 3];
+    float u4;
+    if constexpr (VEC) {
+      // the chunk i+4 .. i+7 is read before any of it is written (writes reach
+      // sample i at most)
+      if ((i & 3) == 0 && i + 4 < CH) ahead = run[i / 4 + 1];
+      const int k = i & 3;
+      u4 = (i + 4 < CH) ? (k == 0 ? ahead.x : k == 1 ? ahead.y : k == 2 ? ahead.z : ahead.w)
+                        : hp[(i + 4 - CH) & 3];
+    } else {
+      u4 = (i + 4 < CH) ? col.get(t + 4) : hp[(i + 4 - CH) & 3];
+    }
     float sC = sl(w2, w3, u4);                    // slope at t+3
     if (i >= CH - 4 && !nl) sC = 0.f;             // t+3 >= nT-1
     const float F2 = kt_fh(w2 + 0.5f * sB, w3 - 0.5f * sC);  // flux at t+5/2
@@ -419,7 +457,16 @@ ASG_DEV void kt_step_stream(const Col& col, float ndt, float dz, unsigned mask) 
     const float G1 = kt_fh(r0 + 0.5f * q0, r1 - 0.5f * q1);  // flux of s1 at t+1/2
     float out = 0.5f * w0 + 0.5f * (r0 + c * (G1 - G));
     if ((i == 0 && !nf) || (i == CH - 1 && !nl)) out = w0;    // column ends
-    col.set(t, out);
+    if constexpr (VEC) {
+      const int k = i & 3;
+      if (k == 0) ahead.x = out;
+      else if (k == 1) ahead.y = out;
+      else if (k == 2) ahead.z = out;
+      else ahead.w = out;
+      if (k == 3) run[i / 4] = ahead;
+    } else {
+      col.set(t, out);
+    }
     w0 = w1; w1 = w2; w2 = w3; w3 = u4;
     sA = sB; sB = sC; F = F2;
     r0 = r1; r1 = r2; q0 = q1; G = G1;
