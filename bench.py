@@ -305,7 +305,9 @@ def run_gpu_arm(args):
     value = world * V * args.steps / (ms / 1e3)
 
     # e2e: public API, host buffers in and out, K steps; the input field in
-    # page-locked host memory, two untimed calls first (host allocator warm-up)
+    # page-locked host memory, two untimed calls first (host allocator warm-up;
+    # the library keeps the plan of the last call with the same grid and
+    # options, so the timed call reuses it: phases_s.plan_reused)
     e2e_s, h2d, d2h = float("nan"), 0, 0
     e2e_phases = None
     if not args.no_e2e:
