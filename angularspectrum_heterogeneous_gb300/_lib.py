@@ -75,7 +75,7 @@ class Tuning(C.Structure):
     _fields_ = [("t_cols_flux", C.c_int), ("t_cols_plain", C.c_int),
                 ("t_cols_stats", C.c_int), ("xy_clusters", C.c_int),
                 ("xy_clusters_closing", C.c_int), ("xy_sync", C.c_int),
-                ("t_prefetch", C.c_int), ("xy_bulk", C.c_int)]
+                ("t_prefetch", C.c_int), ("xy_bulk", C.c_int), ("xy_rows", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

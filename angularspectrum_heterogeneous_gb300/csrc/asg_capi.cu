@@ -230,6 +230,8 @@ struct asg_plan {
   int xy_bulk = 1;            // HBM row loads of the L2 plane kernels (XYParams::bulk_rows);
                               // set from default_bulk() at plan creation
   int t_prefetch = 0;         // column passes: L2 prefetch of a later tile (TParams::prefetch)
+  int xy_rows = 0;            // rows per diffraction CTA in a cooperative launch (asg_tuning
+                              // xy_rows: 0 default, 1 sixteen, 2 eight)
   int xy_sync = 0;            // group barrier of the L2 plane kernels: 0 default,
                               // 1 thread-block cluster, 2 counters in a cooperative launch
   int batch_refs = 0;         // batches holding the plan (they use cluster barriers)
@@ -950,6 +952,7 @@ static XYParams xyparams(asg_plan* p, const float2* table, bool zero_dc_nyq) {
   x.coop = xy_sync_of(p) >= 2 ? 1 : 0;
   x.pipe = xy_sync_of(p) == 3 ? 1 : 0;
   x.bulk_rows = p->xy_bulk;
+  x.rows8 = p->xy_rows != 1 ? 1 : 0;  // used from 256-wide planes in cooperative launches
   x.grp_cnt = p->grp_cnt;
   x.grp_skew = p->barrier_skew;
   x.spec_tmp = p->spec2;
@@ -1715,6 +1718,7 @@ extern "C" int asg_get_tuning(asg_plan* p, asg_tuning* out) {
   out->xy_clusters_closing = p->l2 ? ncl : 0;
   out->xy_sync = xy_sync_of(p);
   out->xy_bulk = p->l2 ? p->xy_bulk + 1 : 0;
+  out->xy_rows = (p->l2 && p->Y >= 256) ? (p->xy_rows == 1 ? 1 : 2) : 0;
   out->t_prefetch = p->tfast ? p->t_prefetch + 1 : 0;
   return ASG_OK;
 }
@@ -1735,6 +1739,7 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
                 t->xy_clusters_closing, L2_MAX_CLUSTERS);
   if (t->xy_sync < 0 || t->xy_sync > 3) return fail(ASG_ERR_ARG, "xy_sync %d outside 0..3", t->xy_sync);
   if (t->xy_bulk < 0 || t->xy_bulk > 3) return fail(ASG_ERR_ARG, "xy_bulk %d outside 0..3", t->xy_bulk);
+  if (t->xy_rows < 0 || t->xy_rows > 2) return fail(ASG_ERR_ARG, "xy_rows %d outside 0..2", t->xy_rows);
   if (t->t_prefetch < 0 || t->t_prefetch > 2)
     return fail(ASG_ERR_ARG, "t_prefetch %d outside 0..2", t->t_prefetch);
   for (int i = 0; i < 3; ++i) p->t_cols[i] = cols[i];
@@ -1742,6 +1747,7 @@ extern "C" int asg_set_tuning(asg_plan* p, const asg_tuning* t) {
   p->xy_clusters_c = t->xy_clusters_closing;
   p->xy_sync = t->xy_sync;
   p->xy_bulk = t->xy_bulk == 0 ? default_bulk(p) : t->xy_bulk - 1;
+  p->xy_rows = t->xy_rows;
   p->t_prefetch = t->t_prefetch == 0 ? 0 : t->t_prefetch - 1;
   p->gen++;
   return ASG_OK;
@@ -1820,6 +1826,22 @@ extern "C" int asg_autotune(asg_plan* p, const float* field, double dz, int step
       }
     }
     p->xy_sync = best_s;
+  }
+  if (p->l2 && p->Y >= 256 && xy_sync_of(p) >= 2 && status == ASG_OK) {
+    // tile shape of the cooperative diffraction kernel: 16-row or 8-row CTAs
+    double best = 1e300;
+    int best_r = 2;
+    for (int r : {1, 2}) {
+      p->xy_rows = r;
+      double ms = 0.0;
+      status = trial(p->cfg.split_step ? ASG_K_XY_B : ASG_K_XY_A, &ms);
+      if (status != ASG_OK) break;
+      if (ms < best) {
+        best = ms;
+        best_r = r;
+      }
+    }
+    p->xy_rows = best_r;
   }
   if (p->l2 && status == ASG_OK) {
     double best = 1e300;

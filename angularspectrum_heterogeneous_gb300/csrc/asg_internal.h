@@ -109,6 +109,8 @@ struct XYParams {
   int skip_plane;          // closing-stage kernel: plane left without epilogue (-1: none)
   int bulk_rows;           // L2-exchange kernels' HBM row loads: 0 cp.async, 1 bulk copies in
                            // the diffraction kernel, 2 bulk copies in both kernels
+  int rows8;               // 1: a cooperative launch of the diffraction kernel uses 8-row CTAs
+                           //    of 4 warps (planes from 256 wide), 0: 16-row CTAs of 8 warps
 };
 
 bool asg_xy_fast_supported(int X, int Y, int* G_out);

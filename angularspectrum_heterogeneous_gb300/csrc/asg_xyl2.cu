@@ -1118,7 +1118,7 @@ static int launch_l2(const XYParams& pin, cudaStream_t st) {
 template <int Yn, int Xn>
 static int launch_l2_mode(const XYParams& p, cudaStream_t st) {
   if constexpr (Yn >= 256) {
-    if (p.coop && !p.power_only) return launch_l2<Yn, Xn, 8, 128>(p, st);
+    if (p.coop && !p.power_only && p.rows8) return launch_l2<Yn, Xn, 8, 128>(p, st);
   }
   return launch_l2<Yn, Xn, 16, 256>(p, st);
 }

@@ -214,6 +214,9 @@ typedef struct {
                       * completion) in the diffraction kernel, 3 bulk copies in the
                       * closing-stage kernel too; 0 = default (1 from 256-wide planes,
                       * where cooperative launches run 8-row CTAs, else 2) */
+  int xy_rows;       /* rows per CTA of the diffraction kernel in a cooperative launch
+                      * (planes from 256 wide): 1 sixteen (8 warps), 2 eight (4 warps,
+                      * twice the CTAs per SM); 0 = default (2).  Clusters use 16. */
 } asg_tuning;
 
 /* Test hook (no counterpart in the reference): adds `skew` to every target of

@@ -39,11 +39,13 @@ def test_every_shape_gives_the_same_march(shape, flux):
         shapes = [dict(t_cols_flux=8, t_cols_plain=8, t_cols_stats=8, xy_clusters=0,
                        xy_clusters_closing=2, xy_sync=1, xy_bulk=1),
                   dict(t_cols_flux=16, t_cols_plain=16, t_cols_stats=16, xy_clusters=3,
-                       xy_clusters_closing=0, xy_sync=2, xy_bulk=3, t_prefetch=2),
+                       xy_clusters_closing=0, xy_sync=2, xy_bulk=3, t_prefetch=2, xy_rows=1),
                   dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
                        xy_clusters_closing=0, xy_sync=2),
                   dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=5,
-                       xy_clusters_closing=0, xy_sync=3, xy_bulk=2)]
+                       xy_clusters_closing=0, xy_sync=3, xy_bulk=2, xy_rows=2),
+                  dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
+                       xy_clusters_closing=0, xy_sync=3, xy_rows=1)]
         for tun in shapes:
             plan.set_tuning(tun)
             got = plan.get_tuning()
