@@ -103,3 +103,39 @@ def test_device_entry_reports_capped_subcycles():
             assert n.value > 0 and need.value > cap, (n.value, need.value)
         else:
             assert n.value == 0, n.value
+
+
+def test_device_entry_records_into_a_cuda_graph():
+    """Global-mode stream capture rejects cudaMalloc, cudaFree and synchronising
+    calls: after one direct call (which loads the kernels), a call recorded into
+    a CUDA graph runs nothing while capturing, and the replay gives the direct
+    call's result."""
+    import torch
+    from angularspectrum_heterogeneous_gb300 import _lib
+    lib = _lib.load()
+    ncols, nT = 37, 256
+    cols = _columns(ncols, nT)
+    dz, dt = 4e-4, 1e-8
+    flux = _lib.FLUX_KT
+    ref = _lib.flux_columns(cols, flux, N_COEF, dz, dt, cfl_target=0.3)
+    s = torch.cuda.Stream()
+    d_in = torch.from_numpy(cols).cuda()
+    d_out = torch.full_like(d_in, float("nan"))
+    torch.cuda.synchronize()
+    _lib.check(_device_call(lib, d_in, d_out, ncols, nT, flux, dz, dt, cfl_target=0.3,
+                            stream=s.cuda_stream))
+    s.synchronize()
+    direct = d_out.clone()
+    d_out.fill_(float("nan"))
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = _device_call(lib, d_in, d_out, ncols, nT, flux, dz, dt, cfl_target=0.3,
+                          stream=s.cuda_stream)
+    _lib.check(rc)
+    torch.cuda.synchronize()
+    assert torch.isnan(d_out).all(), "the captured call ran during capture"
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(d_out, direct)
+    assert rel(d_out.cpu().numpy(), ref) < 1e-6
