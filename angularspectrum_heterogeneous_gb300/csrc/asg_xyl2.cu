@@ -796,31 +796,36 @@ __global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2c(XYPara
         for (int b = 0; b < PX::N2; ++b) t[(b + PX::N2 * ka) * TS + c] = v[b];
       }
       __syncthreads();
-      for (int it = tid; it < 2 * PX::N2 * YR; it += NT) {
-        const int hb = it / YR, c = it - hb * YR;
-        const int h = hb / PX::N2, b = hb - h * PX::N2;
-        float2* t = tile + h * Xs * TS;
-        float2 v[PX::N1];
-        v[0] = t[b * TS + c];
+      // inverse step A of both halves for task (b, c), then on the task's own
+      // x = b + N2x*a, in registers, the recombination s(x) = a + W_X^-x b,
+      // s(x + Xs) = a - W_X^-x b (+ damping x factor): tile h=0 <- s(x),
+      // h=1 <- s(x + Xs)
+      for (int it = tid; it < PX::N2 * YR; it += NT) {
+        const int b = it / YR, c = it - b * YR;
+        float2* ta = tile;
+        float2* tb = tile + Xs * TS;
+        float2 va[PX::N1], vb[PX::N1];
+        va[0] = ta[b * TS + c];
+        vb[0] = tb[b * TS + c];
 #pragma unroll
-        for (int ka = 1; ka < PX::N1; ++ka) v[ka] = cmulc(t[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
-        dft<PX::N1, true>(v);
-#pragma unroll
-        for (int a = 0; a < PX::N1; ++a) t[(b + PX::N2 * a) * TS + c] = v[a];
-      }
-      __syncthreads();
-      // recombination (+ damping x factor): tile h=0 <- s(x), h=1 <- s(x + Xs)
-      for (int i = tid; i < Xs * YR; i += NT) {
-        const int x = i / YR, c = i - x * YR;
-        const float2 a = tile[x * TS + c];
-        const float2 wb = cmulc(tile[(Xs + x) * TS + c], __ldg(p.twX + x));
-        float2 s0 = cadd(a, wb), s1 = csub(a, wb);
-        if (fw && epi) {
-          s0 = cscale(s0, gxs[x]);
-          s1 = cscale(s1, gxs[x + Xs]);
+        for (int ka = 1; ka < PX::N1; ++ka) {
+          va[ka] = cmulc(ta[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
+          vb[ka] = cmulc(tb[(b + PX::N2 * ka) * TS + c], tw_x[b * ka]);
         }
-        tile[x * TS + c] = s0;
-        tile[(Xs + x) * TS + c] = s1;
+        dft<PX::N1, true>(va);
+        dft<PX::N1, true>(vb);
+#pragma unroll
+        for (int a = 0; a < PX::N1; ++a) {
+          const int x = b + PX::N2 * a;
+          const float2 wb = cmulc(vb[a], __ldg(p.twX + x));
+          float2 s0 = cadd(va[a], wb), s1 = csub(va[a], wb);
+          if (fw && epi) {
+            s0 = cscale(s0, gxs[x]);
+            s1 = cscale(s1, gxs[x + Xs]);
+          }
+          ta[x * TS + c] = s0;
+          tb[x * TS + c] = s1;
+        }
       }
       __syncthreads();
       if (sa && epi) {
