@@ -12,7 +12,7 @@ small scenarios and writes the inputs and outputs to ``*.npz`` files next to
 this script.
 
 The fixtures are small on purpose (a few hundred KB in total) and are
-committed; the GPU machine never needs the reference.  Two precisions are
+committed; the GPU tests never need the reference.  Two precisions are
 produced: ``fp32`` runs the module as shipped; ``fp64`` remaps the module's
 float32/complex64 casts to float64/complex128 (the FP64 oracle).
 
