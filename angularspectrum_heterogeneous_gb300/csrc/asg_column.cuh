@@ -468,7 +468,7 @@ ASG_DEV void kt_step_stream(const Col& col, float ndt, float dz, unsigned mask) 
     float q1 = sl(r0, r1, r2);                    // slope of s1 at t+1
     if (i >= CH - 2 && !nl) q1 = 0.f;
     const float G1 = kt_fh(r0 + q0, r1 - q1);  // flux of s1 at t+1/2
-    float out = 0.5f * w0 + 0.5f * (r0 + c * (G1 - G));
+    float out = 0.5f * (w0 + (r0 + c * (G1 - G)));  // = w0/2 + (...)/2: the halvings are exact
     if ((i == 0 && !nf) || (i == CH - 1 && !nl)) out = w0;    // column ends
     if constexpr (VEC) {
       const int k = i & 3;

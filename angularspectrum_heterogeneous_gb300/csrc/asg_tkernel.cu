@@ -147,12 +147,14 @@ __global__ void __launch_bounds__(256, ((PL::N >= 512 || C == 16) ? 3 : 4))
           const float2 xk = side ? xb : xa;
           const float2 xm = side ? mb : ma;
           float2* line = side ? lb : la;
-          const float2 E = make_float2(0.5f * (xk.x + xm.x), 0.5f * (xk.y - xm.y));
-          const float2 D = make_float2(0.5f * (xk.x - xm.x), 0.5f * (xk.y + xm.y));
+          // E and D here are twice the even/odd parts: the halving folds into the
+          // final 1/M scaling (power-of-two scalings are exact)
+          const float2 E = make_float2(xk.x + xm.x, xk.y - xm.y);
+          const float2 D = make_float2(xk.x - xm.x, xk.y + xm.y);
           const float2 O = cmulc(D, wk);
           // Z[k] = E + iO ; Z[M-k] = conj(E) + i conj(O)
-          line[PL::pos(sk)] = make_float2((E.x - O.y) * (2.f * inv2M), (E.y + O.x) * (2.f * inv2M));
-          line[PL::pos(sk2)] = make_float2((E.x + O.y) * (2.f * inv2M), (-E.y + O.x) * (2.f * inv2M));
+          line[PL::pos(sk)] = make_float2((E.x - O.y) * inv2M, (E.y + O.x) * inv2M);
+          line[PL::pos(sk2)] = make_float2((E.x + O.y) * inv2M, (-E.y + O.x) * inv2M);
         }
       }
       }
@@ -253,17 +255,19 @@ __global__ void __launch_bounds__(256, ((PL::N >= 512 || C == 16) ? 3 : 4))
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         const float2* line = lines + (u + CY * side) * LS;
+        // r0, r1: twice the bins k and M-k (the halvings of the even/odd parts
+        // fold into the output scaling below; power-of-two scalings are exact)
         float2 r0, r1;
         if (k == 0) {
           const float2 z = line[PL::pos(0)];
-          r0 = make_float2(z.x + z.y, 0.f);
-          r1 = make_float2(z.x - z.y, 0.f);
+          r0 = make_float2(2.f * (z.x + z.y), 0.f);
+          r1 = make_float2(2.f * (z.x - z.y), 0.f);
         } else {
           const float2 zk = line[PL::pos(sk)];
           const float2 zm = line[PL::pos(sk2)];
-          const float2 E = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-          const float2 D = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y + zm.y));
-          const float2 O = make_float2(D.y, -D.x);  // -i/2 (zk - conj zm)
+          const float2 E = make_float2(zk.x + zm.x, zk.y - zm.y);
+          const float2 D = make_float2(zk.x - zm.x, zk.y + zm.y);
+          const float2 O = make_float2(D.y, -D.x);  // -i (zk - conj zm)
           const float2 WO = cmul(O, wk);
           r0 = make_float2(E.x + WO.x, E.y + WO.y);
           r1 = make_float2(E.x - WO.x, -(E.y - WO.y));
@@ -276,10 +280,16 @@ __global__ void __launch_bounds__(256, ((PL::N >= 512 || C == 16) ? 3 : 4))
         // side s = a +/- W_X^-x b then inverts it exactly
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-          const float2 a = cscale(cadd(ra[j], rb[j]), 0.5f);
-          const float2 b = cmul(csub(ra[j], rb[j]), make_float2(0.5f * wx.x, 0.5f * wx.y));
+          const float2 a = cscale(cadd(ra[j], rb[j]), 0.25f);
+          const float2 b = cmul(csub(ra[j], rb[j]), make_float2(0.25f * wx.x, 0.25f * wx.y));
           ra[j] = a;
           rb[j] = b;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          ra[j] = cscale(ra[j], 0.5f);
+          rb[j] = cscale(rb[j], 0.5f);
         }
       }
       oa[h][0] = ra[0];
