@@ -50,7 +50,7 @@ B_ALG = 48.0  # algorithmic bytes per voxel-step of the Strang path (3 stages x 
 # options: the plane passes on a 512 x 512 x 256 grid (the workload's planes),
 # the column passes on 256 x 256 x 1024 (its columns); the traffic scales with
 # the voxel count.
-DRAM_BYTES_PER_VOXEL = {"xy_A": 10.83, "xy_B": 10.89, "xy_C": 11.48, "t_nonlin": 7.27,
+DRAM_BYTES_PER_VOXEL = {"xy_A": 10.87, "xy_B": 10.90, "xy_C": 11.55, "t_nonlin": 7.25,
                         "t_mid": 7.19, "t_end": 7.22}
 B_SWEEP = 8.0  # algorithmic bytes per voxel of one pass (read 4 + write 4)
 METRIC = "voxel-steps/s"
