@@ -541,7 +541,8 @@ static int plan_create_impl(const asg_config* cfg, asg_plan* p) {
         const int kxs = (sl / n2) + n1 * (sl % n2);  // bin of the Xs-point FFT in slot sl
         const int kx = 2 * kxs + h;
         const int i = (kx + X / 2) % X;
-        cl[h * Xs + sl] = i < X - 1 - i ? i : X - 1 - i;
+        // the class's row offset in the (x class, y class) multiplier tables
+        cl[h * Xs + sl] = (i < X - 1 - i ? i : X - 1 - i) * p->ncy;
       }
     CKS(dalloc(&p->l2_cls_x, 2 * Xs));
     CKS(h2d(p->l2_cls_x, cl.data(), 2 * Xs, p->st));

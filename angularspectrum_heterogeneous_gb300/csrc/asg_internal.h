@@ -96,7 +96,8 @@ struct XYParams {
   const int* step;
   // L2-exchange plane kernel
   float2* l2_scratch;      // [clusters][2][Xs][Y]
-  const int* l2_cls_x;     // [nsub][Xs] class of each x slot of the Xs-point FFT
+  const int* l2_cls_x;     // [nsub][Xs] x class of each slot of the Xs-point FFT times ncy
+                           //    (its row offset in the multiplier tables)
   int l2_buf_elems;        // set by the launcher
   int l2_max_clusters;     // clusters the scratch was sized for
   int coop;                // 1: CTA groups of a cooperative launch synchronised by

@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2(XYParam
         const float* ot = p.obl_table + (size_t)plane * p.ncx * p.ncy + cy;
 #pragma unroll
         for (int kb = 0; kb < PX::N2; ++kb) {
-          const float o = ot[(size_t)cxh[kb + PX::N2 * ka] * p.ncy];
+          const float o = ot[cxh[kb + PX::N2 * ka]];
           const float P = v[kb].x * v[kb].x + v[kb].y * v[kb].y;
           psum = fmaf(P, o, psum);
           pden += (o > 0.f) ? P : 0.f;
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2(XYParam
         const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + cy;
 #pragma unroll
         for (int kb = 0; kb < PX::N2; ++kb)
-          v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
+          v[kb] = cmul(v[kb], tt[cxh[kb + PX::N2 * ka]]);
       } else {
         const float nrm = 1.0f / ((float)Xs * (float)Y);
 #pragma unroll
@@ -785,7 +785,7 @@ __global__ void __launch_bounds__(NT, L2Shape<PY, NT>::kMinBlocks) xy_l2c(XYPara
           const float2* tt = p.table + (size_t)plane * p.ncx * p.ncy + clsy[c0 + c];
 #pragma unroll
           for (int kb = 0; kb < PX::N2; ++kb)
-            v[kb] = cmul(v[kb], tt[(size_t)cxh[kb + PX::N2 * ka] * p.ncy]);
+            v[kb] = cmul(v[kb], tt[cxh[kb + PX::N2 * ka]]);
         } else {
           const float nrm = 1.0f / ((float)Xs * (float)Y);
 #pragma unroll
