@@ -74,6 +74,9 @@ def test_unsupported_shape_is_rejected():
             plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=12, t_cols_stats=0, xy_clusters=0))
         with pytest.raises(ASGError):
             plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=99))
+        with pytest.raises(ASGError):
+            plan.set_tuning(dict(t_cols_flux=0, t_cols_plain=0, t_cols_stats=0, xy_clusters=0,
+                                 xy_rows=3))
     finally:
         plan.close()
 
