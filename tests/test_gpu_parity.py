@@ -201,12 +201,15 @@ FAST_CASES = {
                          dict(zs=[5.0e-4])),
     "big_odd_obl": ((129, 127, 48), dict(fluxScheme="kt", useNonlinearityObliquity=True),
                     4e6, 3),
-    # groups of 8 CTAs: plane kernels in a cooperative launch with counter barriers,
-    # with the beam-obliquity power pass (its extra barrier) in the second case
+    # 256-wide planes: plane kernels in a cooperative launch with counter barriers
+    # (diffraction passes with 8-row CTAs in groups of 16, the closing pass and the
+    # beam-obliquity power pass with 16-row CTAs in groups of 8), and the Lie march's
+    # combined diffraction-attenuation multiplier on the 8-row kernel
     "kt_fw_sa_256_coop": ((256, 256, 128), dict(fluxScheme="kt", useFreqWeightedBoundary=True,
                                                 useSuperAbsorbing=True), 4e6, 2),
     "kt_obl_256_coop": ((256, 256, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
                         4e6, 2),
+    "lie_water_256_coop": ((256, 256, 128), dict(useSplitStep=False, alpha0=-1.0), 3e6, 2),
     "kt_obl_32x64": ((32, 64, 128), dict(fluxScheme="kt", useNonlinearityObliquity=True),
                      6e6, 8),
     # half-plane (split-x) kernels with the beam-obliquity power pass
