@@ -1,10 +1,12 @@
 // Plane kernel with the x exchange through an L2-resident scratch.
 //
-// A group of G CTAs owns one (half-)plane of Xs x Y modes at a time
+// A group of G = Xs/R CTAs owns one (half-)plane of Xs x Y modes at a time
 // (persistent, planes strided by the group count).  The group is a
-// thread-block cluster, or, for G >= 12, G consecutive CTAs of a cooperative
-// launch that meet at counter barriers in global memory (a 16-CTA cluster must
-// fit in one GPC, which leaves a quarter of the SMs idle):
+// thread-block cluster (R = 16 rows per CTA), or G consecutive CTAs of a
+// cooperative launch that meet at counter barriers in global memory (a 16-CTA
+// cluster must fit in one GPC, which leaves a quarter of the SMs idle); from
+// 256-wide planes a cooperative launch of the diffraction kernel uses R = 8
+// rows per 4-warp CTA, twice the CTAs per SM:
 //   1. each CTA loads R rows (cp.async, prefetched during the previous
 //      plane), runs the forward y FFT in shared memory and writes the rows to
 //      the group's scratch buffer in global memory (it stays in L2);
@@ -15,9 +17,10 @@
 //   3. group barrier; each CTA reads its rows back, runs the inverse y FFT
 //      and stores the rows to HBM.
 // One scratch half-plane per group suffices with two barriers per plane:
-// stages 1 and 3 of a CTA touch only its own rows.  Shared memory holds either R rows
-// or Xs x Yc columns, both about 64 KB for 512 x 512 planes split in halves,
-// so two CTAs share an SM.
+// stages 1 and 3 of a CTA touch only its own rows (the split-phase flow uses
+// two).  Shared memory holds either R rows or Xs x Yc columns: about 64 KB
+// with 16 rows for 512 x 512 planes split in halves (two CTAs per SM), 32 KB
+// with 8 rows (four CTAs per SM).
 //
 // Reference semantics are those of the plane kernels in asg_xykernel.cu
 // (angular_spectrum_solver.py :649-655, :667-685, :630-643).
