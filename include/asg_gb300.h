@@ -206,7 +206,8 @@ typedef struct {
                       * block runs the next plane's first stage, or this plane's last,
                       * between arriving at a barrier and waiting on it); the launch is sized to fill the GPU
                       * (plans in a batch use 1; so should a plan whose stream runs
-                      * beside other heavy work on the same GPU) */
+                      * beside other heavy work on the same GPU); 0 = default (3 from
+                      * 256-wide planes and for groups of 12 or more CTAs, else 1) */
   int t_prefetch;    /* column passes: 1 none, 2 each block prefetches into L2 the spectrum of
                       * the tile that starts about one block lifetime later; 0 = default (1) */
   int xy_bulk;       /* HBM row loads of those kernels: 1 16-byte cp.async per lane, 2 bulk
